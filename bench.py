@@ -1,0 +1,355 @@
+"""GTEPS benchmark of the DAWN frontier path on GB300.
+
+Workload (one "step"): hop distances from 64 seeded sources of a symmetrised
+RMAT scale-22 graph (edge factor 16, a=.57 b=.19 c=.19 d=.05, deduplicated,
+self loops removed, seeded vertex relabelling), int32 CSR resident in HBM,
+int32 distances (nsrc x n) written to HBM.  The graph and sources are
+seeded synthetic data with the benchmark's shapes.
+
+  value      whole-job GTEPS of the batched bitset traversal (CSR already
+             resident, distances left on the device), CUDA events on the
+             traversal stream around exactly --steps steps
+  e2e        the same metric through the C ABI with host buffers: per step
+             dawn_graph_create from pinned host CSR + dawn_bfs into a pinned
+             host array + dawn_graph_destroy
+  plain      the same 64 sources through the single-source
+             direction-optimising kernels (for the batched-vs-plain ratio)
+  roofline   the dominant kernel's algorithmic bytes per launch / its
+             CUDA-event launch time, from a traced replay of one step
+  cpu_baseline  the reference CPU path (MSSP_CPU::run restated, OpenMP over
+             sources, serial queue BFS each) on a bounded sample of sources
+
+Multi-GPU: sources shard across ranks (each rank its own 64 sources on its
+own replica of the graph, no collective on the data path), weak scaling.
+`--impl reference` times the reference CPU implementation instead.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gal-dawn_gb300"))
+
+SCALE, EDGEFACTOR, A, B, C = 22, 16, 0.57, 0.19, 0.19
+GRAPH_SEED, SOURCE_SEED, NSRC = 2022, 64, 64
+METRIC = "GTEPS per GB300 (BFS/SSSP/MSSP) learned+batched vs plain; % HBM roofline"
+L2_BYTES = 129 * 2 ** 20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_workload(scale, rank):
+    from dawn_gb300 import gen
+    t = time.time()
+    g = gen.rmat(scale, EDGEFACTOR, A, B, C, seed=GRAPH_SEED)
+    srcs = gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
+    log(f"[bench] rmat{scale}: n={g.n} m={g.m} generated in {time.time() - t:.1f}s")
+    return g, srcs
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples (every 50 ms) from the warm-up through the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 6:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[2:6]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def time_steps(torch, fn, steps, warmup, barrier):
+    for _ in range(warmup):
+        fn()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    barrier()
+    return e0.elapsed_time(e1)
+
+
+def bitset_roofline(dg, g, srcs, d_dist, abi, peak_gbs, peak_kind):
+    """Traced replay of one step: per-kernel CUDA-event durations, and the
+    algorithmic bytes of each launch of the dominant kernel."""
+    dg.trace(True)
+    dg.bfs_device(srcs, d_dist, variant=abi.VARIANT_BITSET, stats=False)
+    dg.synchronize()
+    recs = dg.trace_read()
+    dg.trace(False)
+    per = {}
+    for r in recs:
+        k = per.setdefault(r["kernel"], {"launches": 0, "ms": 0.0, "bytes": 0})
+        k["launches"] += 1
+        k["ms"] += r["ms"]
+        k["bytes"] += alg_bytes(r, g.n, g.m)
+    total = sum(k["ms"] for k in per.values())
+    dom = max(per, key=lambda k: per[k]["ms"])
+    k = per[dom]
+    avg_ms = k["ms"] / k["launches"]
+    avg_bytes = k["bytes"] / k["launches"]
+    achieved = avg_bytes / (avg_ms * 1e-3) / 1e9
+    share = {name: round(v["ms"] / total, 4) for name, v in per.items()}
+    return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak_gbs,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
+            "traffic": None, "launches_per_step": k["launches"], "avg_launch_ms": round(avg_ms, 4),
+            "alg_bytes_per_launch": int(avg_bytes), "kernel_share": share,
+            "source": "CUDA events around each kernel in a traced replay of one step"}, recs
+
+
+def alg_bytes(r, n, m):
+    """Algorithmic HBM bytes of one kernel launch (bitset traversal, 64 sources).
+
+    bs_pull (one level sweep): row_ptr 4(n+1), visited words read 8n,
+      frontier words written 8n, col of the unfinished rows 4*mu.
+    bs_push_scatter: row_ptr + col of the frontier rows 4*(nf + mf).
+    bs_push_update:  visited/next/frontier words of the touched vertices, bounded by 24*mf.
+    Distance writes (4 bytes per newly reached pair) are added per level by
+    the kernel that finds them; they are not visible in a level record and
+    are counted once per step in the step-level figure instead.
+    """
+    k = r["kernel"]
+    if k == "bs_pull":
+        return 4 * (n + 1) + 16 * n + 4 * r["unvisited_edges"]
+    if k == "bs_push_scatter":
+        return 4 * (r["frontier"] + r["frontier_edges"])
+    if k == "bs_push_update":
+        return 24 * min(r["frontier_edges"], n)
+    if k == "bfs_pull":
+        return 4 * (n + 1) + n // 8 + 4 * r["unvisited_edges"]
+    if k == "bfs_push":
+        return 4 * (r["frontier"] + r["frontier_edges"])
+    return 0
+
+
+def _cpu_impl():
+    """The reference CPU path: compiled from the reference's own sources when
+    that build loads here, else the oracle's restatement of it."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    threads = os.cpu_count() or 1
+    if O.ref_available():
+        return O, "reference", threads, lambda g, s: O.ref_mssp(g, s, want_dist=False)
+    return O, "port", threads, lambda g, s: O.mssp(g, s, threads=threads, want_dist=False)
+
+
+def cpu_baseline(g, srcs):
+    """All sources once through MSSP_CPU::run (OpenMP over sources, one
+    serial queue BFS each), wall-clock timed."""
+    O, kind, threads, run = _cpu_impl()
+    edges = O.mssp(g, srcs[:1], threads=1, want_dist=False)[1]  # loads the port
+    edges = O.mssp(g, srcs, threads=threads, want_dist=False)[1] if kind == "reference" else None
+    t0 = time.perf_counter()
+    out = run(g, srcs)
+    dt = time.perf_counter() - t0
+    if edges is None:
+        edges = out[1]
+    return {"value": round(edges / dt / 1e9, 4), "unit": "GTEPS", "cores": threads, "kind": kind,
+            "sample": f"all {len(srcs)} sources once ({dt:.1f} s wall, {threads} threads)"}
+
+
+def run_reference_arm(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    g, srcs = make_workload(args.scale, 0)
+    O, kind, threads, run = _cpu_impl()
+    # Per step: one wave of sources (one per thread), fewer when --steps is
+    # large, so the whole run stays within about three minutes.
+    one = time.perf_counter()
+    O.mssp(g, srcs[:1], threads=1, want_dist=False)
+    one = time.perf_counter() - one
+    per_step = max(1, min(len(srcs), threads))
+    if (args.steps + args.warmup) * one > 180:
+        per_step = 1
+    sample = srcs[:per_step]
+    edges = O.mssp(g, sample, threads=threads, want_dist=False)[1]
+    for _ in range(args.warmup):
+        run(g, sample)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run(g, sample)
+    dt = time.perf_counter() - t0
+    gteps = edges * args.steps / dt / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded RMAT)",
+            "config": {"workload": f"rmat{args.scale}-ef{EDGEFACTOR}-bfs-{NSRC}src", "n": g.n, "m": g.m,
+                       "sources_per_step": per_step},
+            "cpu_baseline": {"value": round(gteps, 4), "unit": "GTEPS", "cores": threads, "kind": kind,
+                             "sample": f"{per_step} of the {NSRC} sources per step, MSSP_CPU::run"},
+            "e2e": {"value": round(gteps, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="dawn", choices=["dawn", "reference"])
+    ap.add_argument("--scale", type=int, default=SCALE)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--plain-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    from dawn_gb300 import abi
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    barrier = lambda: None  # noqa: E731
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        barrier = dist.barrier
+    g, srcs = make_workload(args.scale, rank)
+    stream = torch.cuda.current_stream().cuda_stream
+    peak_gbs, peak_kind = peaks()
+
+    dg = abi.Graph(g, stream=stream)
+    d_dist = torch.empty((NSRC, g.n), dtype=torch.int32, device="cuda")
+    step = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=False)  # noqa
+    st = dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=True)
+    edges = st.edges_traversed
+
+    clocks = Clocks(local)
+    clocks.start()
+    ms = time_steps(torch, step, args.steps, args.warmup, barrier)
+    clk = clocks.stop()
+    ms_step = ms / args.steps
+    # max over ranks
+    t = torch.tensor([ms_step], device="cuda")
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_step = float(t.item())
+    value = edges * ws / (ms_step * 1e-3) / 1e9
+
+    # plain single-source direction-optimising kernels, same sources
+    step_plain = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_DO, stats=False)  # noqa
+    ms_plain = time_steps(torch, step_plain, args.plain_steps, 1, barrier) / args.plain_steps
+    plain = {"value": round(edges / (ms_plain * 1e-3) / 1e9, 3), "unit": "GTEPS",
+             "ms_per_step": round(ms_plain, 3), "variant": "single-source push/pull (direction-optimising)"}
+
+    roof, recs = bitset_roofline(dg, g, srcs, d_dist.data_ptr(), abi, peak_gbs, peak_kind)
+    step_bytes = 4 * g.m + 4 * (g.n + 1) + NSRC * 4 * g.n
+    roof["step_alg_bytes"] = step_bytes
+    roof["step_achieved"] = round(step_bytes / (ms_step * 1e-3) / 1e9, 1)
+
+    # end to end through the C ABI with pinned host buffers
+    rp_h = torch.from_numpy(g.row_ptr).pin_memory()
+    col_h = torch.from_numpy(g.col).pin_memory()
+    out_h = torch.empty((NSRC, g.n), dtype=torch.int32).pin_memory()
+
+    def e2e_step():
+        h = abi.Graph(raw=dict(n=g.n, m=g.m, row_ptr=rp_h.data_ptr(), col=col_h.data_ptr(), symmetric=True,
+                               stream=stream))
+        h.bfs_host_ptr(srcs, out_h.data_ptr(), variant=abi.VARIANT_BITSET)
+        h.close()
+
+    e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+    h2d = 4 * (g.n + 1) + 4 * g.m + 4 * NSRC
+    d2h = 4 * NSRC * g.n
+    e2e = {"value": round(edges / (e2e_ms * 1e-3) / 1e9 * ws, 3), "unit": "GTEPS", "ms_per_step": round(e2e_ms, 3),
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "call": "dawn_graph_create(pinned host CSR) + dawn_bfs(pinned host dist) + dawn_graph_destroy"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(g, srcs)
+
+    launches = sum(1 for r in recs) + 3  # level kernels + clear/init/next per batch (traced count)
+    line = {"metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
+            "config": {"workload": f"rmat{args.scale}-ef{EDGEFACTOR}-bfs-{NSRC}src-bitset", "n": g.n, "m": g.m,
+                       "sources": NSRC, "edges_traversed_per_step": edges,
+                       "l2": "inputs larger than L2 (CSR %.0f MB, distances %.0f MB per step)" % (
+                           (4 * g.m + 4 * g.n) / 2 ** 20, 4 * NSRC * g.n / 2 ** 20),
+                       "parallelism": f"sources sharded, {ws} replica(s)"},
+            "clocks": clk, "e2e": e2e, "plain": plain,
+            "speedup_vs_plain": round(value / plain["value"], 3) if plain["value"] else None,
+            "roofline": roof, "cpu_baseline": cpu, "gpu_launches": launches * args.steps,
+            "levels_per_step": st.levels, "push_levels": st.push_levels, "pull_levels": st.pull_levels}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dg.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,479 @@
+// extern "C" entry points of libdawn_gb300.so (declared in include/dawn_gb300.h).
+//
+// Argument checking, graph upload, staging of host buffers and statistics
+// live here; the traversals themselves are in bovm.cu (single-source
+// expand), msbfs.cu (64-source bitset expand) and govm.cu (min-plus relax).
+#include <climits>
+#include <cstring>
+#include <vector>
+
+#include "dawn_internal.cuh"
+
+using dawn::DevBuf;
+
+namespace {
+
+constexpr size_t kStageBytes = (size_t)1 << 31;  // host-pointer calls: device staging per chunk
+
+dawn_status check_sources(const dawn_graph* g, const int32_t* sources, int32_t nsrc) {
+  if (nsrc < 0 || (nsrc > 0 && !sources)) {
+    dawn::set_error("invalid source list (nsrc = %d)", nsrc);
+    return DAWN_ERR_INVALID_ARG;
+  }
+  for (int32_t i = 0; i < nsrc; i++)
+    if (sources[i] < 0 || sources[i] >= g->n) {
+      dawn::set_error("source %d (index %d) outside [0, %d)", sources[i], i, g->n);
+      return DAWN_ERR_INVALID_ARG;
+    }
+  return DAWN_OK;
+}
+
+dawn_status finish_graph(dawn_graph* g, uint32_t flags) {
+  if (!(flags & DAWN_GRAPH_NO_VALIDATE)) DAWN_CHECK(dawn::validate_csr(g));
+  if (g->symmetric) {
+    g->t_row_ptr = g->row_ptr;
+    g->t_col = g->col;
+  } else {
+    DAWN_CHECK(dawn::build_transpose(g));
+  }
+  DAWN_CUDA(cudaMallocHost(&g->h_ctl, 2 * sizeof(dawn::SsCtl)));
+  DAWN_CUDA(cudaEventCreate(&g->ev0));
+  DAWN_CUDA(cudaEventCreate(&g->ev1));
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  return DAWN_OK;
+}
+
+dawn_status start_graph(dawn_wtype wtype, int32_t n, int64_t m, uint32_t flags, void* stream, dawn_graph** out,
+                        const void* row_ptr, const void* col, const void* val, dawn_graph** gp) {
+  if (!out) {
+    dawn::set_error("out is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  *out = nullptr;
+  if (n < 1 || m < 0 || m > INT32_MAX || !row_ptr || (m > 0 && !col) ||
+      (wtype != DAWN_W_NONE && wtype != DAWN_W_I32 && wtype != DAWN_W_F32) ||
+      (wtype != DAWN_W_NONE && m > 0 && !val)) {
+    dawn::set_error("invalid graph arguments (n = %d, m = %lld, wtype = %d)", n, (long long)m, (int)wtype);
+    return DAWN_ERR_INVALID_ARG;
+  }
+  dawn_graph* g = new dawn_graph();
+  *gp = g;
+  g->n = n;
+  g->m = m;
+  g->flags = flags;
+  g->wtype = wtype;
+  g->symmetric = (flags & DAWN_GRAPH_SYMMETRIC) != 0;
+  DAWN_CUDA(cudaGetDevice(&g->device));
+  DAWN_CUDA(cudaDeviceGetAttribute(&g->geo.sms, cudaDevAttrMultiProcessorCount, g->device));
+  if (stream) {
+    g->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    DAWN_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    g->own_stream = true;
+  }
+  DAWN_CUDA(cudaMalloc(&g->row_ptr, sizeof(int32_t) * ((size_t)n + 1)));
+  DAWN_CUDA(cudaMalloc(&g->col, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
+  if (wtype != DAWN_W_NONE) DAWN_CUDA(cudaMalloc(&g->val, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
+  return DAWN_OK;
+}
+
+void destroy(dawn_graph* g) {
+  if (!g) return;
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  if (g->t_row_ptr && g->t_row_ptr != g->row_ptr) cudaFree(g->t_row_ptr);
+  if (g->t_col && g->t_col != g->col) cudaFree(g->t_col);
+  cudaFree(g->row_ptr);
+  cudaFree(g->col);
+  if (g->val) cudaFree(g->val);
+  DevBuf* bufs[] = {&g->ss_queues, &g->ss_bitmaps, &g->ss_ctl, &g->ss_sources, &g->ss_scratch,
+                    &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->cc_out, &g->dist_stage};
+  for (DevBuf* b : bufs) dawn::release(*b);
+  if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
+  if (g->sssp_exec) cudaGraphExecDestroy(g->sssp_exec);
+  if (g->bs_exec) cudaGraphExecDestroy(g->bs_exec);
+  if (g->h_ctl) cudaFreeHost(g->h_ctl);
+  for (cudaEvent_t e : g->trace_ev)
+    if (e) cudaEventDestroy(e);
+  if (g->ev0) cudaEventDestroy(g->ev0);
+  if (g->ev1) cudaEventDestroy(g->ev1);
+  if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+  delete g;
+}
+
+int32_t resolve_variant(int32_t variant, int32_t nsrc) {
+  if (variant == DAWN_VARIANT_AUTO) return nsrc >= 2 ? DAWN_VARIANT_BITSET : DAWN_VARIANT_DO;
+  return variant;
+}
+
+dawn_status bfs_device_impl(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,
+                            int32_t variant, dawn_stats* st) {
+  variant = resolve_variant(variant, nsrc);
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
+  }
+  if (variant == DAWN_VARIANT_PUSH || variant == DAWN_VARIANT_DO) {
+    DAWN_CHECK(dawn::bfs_single(g, sources, nsrc, d_dist, variant));
+    if (st) {
+      DAWN_CUDA(cudaEventRecord(g->ev1, g->stream));
+      dawn::SsCtl c;
+      DAWN_CHECK(dawn::download_ctl(g, &c));
+      st->edges_traversed = (int64_t)c.total_reached;
+      st->levels = c.total_levels;
+      st->push_levels = c.total_push;
+      st->pull_levels = c.total_pull;
+      st->batches = nsrc;
+    }
+  } else if (variant == DAWN_VARIANT_BITSET || variant == DAWN_VARIANT_LEARNED) {
+    DAWN_CHECK(dawn::bfs_bitset(g, sources, nsrc, d_dist));
+    if (st) {
+      DAWN_CUDA(cudaEventRecord(g->ev1, g->stream));
+      DAWN_CHECK(dawn::bfs_bitset_stats(g, st, nsrc));
+    }
+  } else {
+    dawn::set_error("unknown BFS variant %d", variant);
+    return DAWN_ERR_UNSUPPORTED;
+  }
+  if (st) {
+    DAWN_CUDA(cudaEventSynchronize(g->ev1));
+    DAWN_CUDA(cudaEventElapsedTime(&st->device_ms, g->ev0, g->ev1));
+  }
+  return DAWN_OK;
+}
+
+dawn_status sssp_device_impl(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist,
+                             dawn_stats* st) {
+  if (st) {
+    std::memset(st, 0, sizeof(*st));
+    DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
+  }
+  DAWN_CHECK(dawn::sssp_single(g, sources, nsrc, d_dist));
+  if (st) {
+    DAWN_CUDA(cudaEventRecord(g->ev1, g->stream));
+    dawn::SsCtl c;
+    DAWN_CHECK(dawn::download_ctl(g, &c));
+    st->levels = c.total_levels;
+    st->push_levels = c.total_push;
+    st->batches = nsrc;
+    DAWN_CUDA(cudaEventElapsedTime(&st->device_ms, g->ev0, g->ev1));
+    // TEPS numerator: out-degree sum of the reached vertices of every row.
+    DAWN_CHECK(dawn::ensure(g->cc_out, 16 * (size_t)nsrc));
+    double* sum = g->cc_out.as<double>();
+    long long* cnt = reinterpret_cast<long long*>(sum + nsrc);
+    DAWN_CHECK(dawn::row_reduce(g, d_dist, nsrc, g->ss_sources.as<int32_t>(), g->wtype == DAWN_W_F32 ? 2 : 1,
+                                1, sum, cnt));
+    std::vector<long long> h(nsrc);
+    DAWN_CUDA(cudaMemcpyAsync(h.data(), sum, sizeof(long long) * nsrc, cudaMemcpyDeviceToHost, g->stream));
+    DAWN_CUDA(cudaStreamSynchronize(g->stream));
+    for (long long x : h) st->edges_traversed += x;
+  }
+  return DAWN_OK;
+}
+
+void add_stats(dawn_stats* acc, const dawn_stats& s) {
+  acc->edges_traversed += s.edges_traversed;
+  acc->levels += s.levels;
+  acc->push_levels += s.push_levels;
+  acc->pull_levels += s.pull_levels;
+  acc->batches += s.batches;
+  acc->device_ms += s.device_ms;
+}
+
+// Runs a device traversal in chunks of sources through device staging and
+// copies each chunk's rows to the caller's host array.
+template <class Fn>
+dawn_status staged(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* host_dist, size_t elem,
+                   dawn_stats* st, Fn&& run) {
+  const size_t row_bytes = elem * (size_t)g->n;
+  int32_t chunk = (int32_t)(kStageBytes / row_bytes);
+  if (chunk >= 64) chunk -= chunk % 64;
+  if (chunk < 1) chunk = 1;
+  if (chunk > nsrc) chunk = nsrc;
+  DAWN_CHECK(dawn::ensure(g->dist_stage, row_bytes * (size_t)chunk));
+  if (st) std::memset(st, 0, sizeof(*st));
+  for (int32_t i0 = 0; i0 < nsrc; i0 += chunk) {
+    const int32_t c = nsrc - i0 < chunk ? nsrc - i0 : chunk;
+    dawn_stats s;
+    DAWN_CHECK(run(sources + i0, c, g->dist_stage.p, st ? &s : nullptr));
+    DAWN_CUDA(cudaMemcpyAsync(static_cast<char*>(host_dist) + row_bytes * (size_t)i0, g->dist_stage.p,
+                              row_bytes * (size_t)c, cudaMemcpyDeviceToHost, g->stream));
+    if (st) add_stats(st, s);
+  }
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  return DAWN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dawn_last_error(void) { return dawn::last_error(); }
+
+const char* dawn_version(void) { return "dawn_gb300 0.1 (sm_103a)"; }
+
+dawn_status dawn_graph_create(const int32_t* row_ptr, const int32_t* col, const void* val, dawn_wtype wtype,
+                              int32_t n, int64_t m, uint32_t flags, void* stream, dawn_graph** out) {
+  dawn::clear_error();
+  dawn_graph* g = nullptr;
+  dawn_status s = start_graph(wtype, n, m, flags, stream, out, row_ptr, col, val, &g);
+  if (s == DAWN_OK) {
+    do {
+      cudaError_t e = cudaMemcpyAsync(g->row_ptr, row_ptr, sizeof(int32_t) * ((size_t)n + 1),
+                                      cudaMemcpyHostToDevice, g->stream);
+      if (e == cudaSuccess && m > 0)
+        e = cudaMemcpyAsync(g->col, col, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, g->stream);
+      if (e == cudaSuccess && m > 0 && g->val)
+        e = cudaMemcpyAsync(g->val, val, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, g->stream);
+      if (e != cudaSuccess) {
+        dawn::set_error("CSR upload: %s", cudaGetErrorString(e));
+        s = DAWN_ERR_CUDA;
+        break;
+      }
+      s = finish_graph(g, flags);
+    } while (0);
+  }
+  if (s != DAWN_OK) {
+    destroy(g);
+    return s;
+  }
+  *out = g;
+  return DAWN_OK;
+}
+
+dawn_status dawn_graph_create_device(const int32_t* d_row_ptr, const int32_t* d_col, const void* d_val,
+                                     dawn_wtype wtype, int32_t n, int64_t m, uint32_t flags, void* stream,
+                                     dawn_graph** out) {
+  dawn::clear_error();
+  dawn_graph* g = nullptr;
+  dawn_status s = start_graph(wtype, n, m, flags, stream, out, d_row_ptr, d_col, d_val, &g);
+  if (s == DAWN_OK) {
+    do {
+      cudaError_t e = cudaMemcpyAsync(g->row_ptr, d_row_ptr, sizeof(int32_t) * ((size_t)n + 1),
+                                      cudaMemcpyDeviceToDevice, g->stream);
+      if (e == cudaSuccess && m > 0)
+        e = cudaMemcpyAsync(g->col, d_col, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToDevice, g->stream);
+      if (e == cudaSuccess && m > 0 && g->val)
+        e = cudaMemcpyAsync(g->val, d_val, sizeof(int32_t) * (size_t)m, cudaMemcpyDeviceToDevice, g->stream);
+      if (e != cudaSuccess) {
+        dawn::set_error("CSR copy: %s", cudaGetErrorString(e));
+        s = DAWN_ERR_CUDA;
+        break;
+      }
+      s = finish_graph(g, flags);
+    } while (0);
+  }
+  if (s != DAWN_OK) {
+    destroy(g);
+    return s;
+  }
+  *out = g;
+  return DAWN_OK;
+}
+
+dawn_status dawn_graph_destroy(dawn_graph* g) {
+  dawn::clear_error();
+  destroy(g);
+  return DAWN_OK;
+}
+
+dawn_status dawn_graph_set_stream(dawn_graph* g, void* stream) {
+  dawn::clear_error();
+  if (!g) {
+    dawn::set_error("graph is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  if (g->own_stream) cudaStreamDestroy(g->stream);
+  g->own_stream = false;
+  if (stream) {
+    g->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    DAWN_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    g->own_stream = true;
+  }
+  return DAWN_OK;
+}
+
+dawn_status dawn_graph_synchronize(dawn_graph* g) {
+  dawn::clear_error();
+  if (!g) {
+    dawn::set_error("graph is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  return DAWN_OK;
+}
+
+dawn_status dawn_bfs_device(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,
+                            int32_t variant, dawn_stats* stats) {
+  dawn::clear_error();
+  if (!g || (nsrc > 0 && !d_dist)) {
+    dawn::set_error("graph or distance buffer is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  DAWN_CHECK(check_sources(g, sources, nsrc));
+  if (nsrc == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return DAWN_OK;
+  }
+  return bfs_device_impl(g, sources, nsrc, d_dist, variant, stats);
+}
+
+dawn_status dawn_bfs(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* dist, int32_t variant,
+                     dawn_stats* stats) {
+  dawn::clear_error();
+  if (!g || (nsrc > 0 && !dist)) {
+    dawn::set_error("graph or distance buffer is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  DAWN_CHECK(check_sources(g, sources, nsrc));
+  if (nsrc == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return DAWN_OK;
+  }
+  return staged(g, sources, nsrc, dist, sizeof(int32_t), stats,
+                [&](const int32_t* s, int32_t c, void* d, dawn_stats* st) {
+                  return bfs_device_impl(g, s, c, static_cast<int32_t*>(d), variant, st);
+                });
+}
+
+dawn_status dawn_sssp_device(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist, int32_t variant,
+                             dawn_stats* stats) {
+  dawn::clear_error();
+  (void)variant;
+  if (!g || (nsrc > 0 && !d_dist)) {
+    dawn::set_error("graph or distance buffer is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (g->wtype == DAWN_W_NONE) {
+    dawn::set_error("dawn_sssp needs a weighted graph");
+    return DAWN_ERR_UNSUPPORTED;
+  }
+  DAWN_CHECK(check_sources(g, sources, nsrc));
+  if (nsrc == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return DAWN_OK;
+  }
+  return sssp_device_impl(g, sources, nsrc, d_dist, stats);
+}
+
+dawn_status dawn_sssp(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* dist, int32_t variant,
+                      dawn_stats* stats) {
+  dawn::clear_error();
+  (void)variant;
+  if (!g || (nsrc > 0 && !dist)) {
+    dawn::set_error("graph or distance buffer is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (g->wtype == DAWN_W_NONE) {
+    dawn::set_error("dawn_sssp needs a weighted graph");
+    return DAWN_ERR_UNSUPPORTED;
+  }
+  DAWN_CHECK(check_sources(g, sources, nsrc));
+  if (nsrc == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return DAWN_OK;
+  }
+  return staged(g, sources, nsrc, dist, sizeof(int32_t), stats,
+                [&](const int32_t* s, int32_t c, void* d, dawn_stats* st) {
+                  return sssp_device_impl(g, s, c, d, st);
+                });
+}
+
+dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t weighted, double* cc,
+                           double* dist_sum, int64_t* reached, dawn_stats* stats) {
+  dawn::clear_error();
+  if (!g || (nsrc > 0 && !cc)) {
+    dawn::set_error("graph or output is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (weighted && g->wtype == DAWN_W_NONE) {
+    dawn::set_error("weighted closeness needs a weighted graph");
+    return DAWN_ERR_UNSUPPORTED;
+  }
+  DAWN_CHECK(check_sources(g, sources, nsrc));
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (nsrc == 0) return DAWN_OK;
+  const int kind = !weighted ? 0 : (g->wtype == DAWN_W_F32 ? 2 : 1);
+  const size_t row_bytes = sizeof(int32_t) * (size_t)g->n;
+  int32_t chunk = (int32_t)(kStageBytes / row_bytes);
+  if (chunk >= 64) chunk -= chunk % 64;
+  if (chunk < 1) chunk = 1;
+  if (chunk > nsrc) chunk = nsrc;
+  DAWN_CHECK(dawn::ensure(g->dist_stage, row_bytes * (size_t)chunk));
+  DAWN_CHECK(dawn::ensure(g->cc_out, 16 * (size_t)chunk));
+  DevBuf srcbuf;
+  DAWN_CHECK(dawn::ensure(srcbuf, sizeof(int32_t) * (size_t)chunk));
+  std::vector<double> hsum(chunk);
+  std::vector<long long> hcnt(chunk);
+  dawn_status s = DAWN_OK;
+  for (int32_t i0 = 0; i0 < nsrc && s == DAWN_OK; i0 += chunk) {
+    const int32_t c = nsrc - i0 < chunk ? nsrc - i0 : chunk;
+    dawn_stats one;
+    if (weighted)
+      s = sssp_device_impl(g, sources + i0, c, g->dist_stage.p, stats ? &one : nullptr);
+    else
+      s = bfs_device_impl(g, sources + i0, c, g->dist_stage.as<int32_t>(), DAWN_VARIANT_AUTO,
+                          stats ? &one : nullptr);
+    if (s != DAWN_OK) break;
+    if (stats) add_stats(stats, one);
+    double* sum = g->cc_out.as<double>();
+    long long* cnt = reinterpret_cast<long long*>(sum + chunk);
+    if (cudaMemcpyAsync(srcbuf.p, sources + i0, sizeof(int32_t) * c, cudaMemcpyHostToDevice, g->stream) !=
+        cudaSuccess) {
+      dawn::set_error("source upload failed");
+      s = DAWN_ERR_CUDA;
+      break;
+    }
+    if ((s = dawn::row_reduce(g, g->dist_stage.p, c, srcbuf.as<int32_t>(), kind, 0, sum, cnt)) != DAWN_OK) break;
+    if (cudaMemcpyAsync(hsum.data(), sum, sizeof(double) * c, cudaMemcpyDeviceToHost, g->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(hcnt.data(), cnt, sizeof(long long) * c, cudaMemcpyDeviceToHost, g->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(g->stream) != cudaSuccess) {
+      dawn::set_error("closeness read-back failed");
+      s = DAWN_ERR_CUDA;
+      break;
+    }
+    for (int32_t i = 0; i < c; i++) {
+      double total;
+      if (kind == 2) {
+        total = hsum[i];
+      } else {
+        long long bits;
+        std::memcpy(&bits, &hsum[i], sizeof(bits));
+        total = (double)bits;
+      }
+      cc[i0 + i] = total > 0 ? (double)(g->n - 1) / total : 0.0;
+      if (dist_sum) dist_sum[i0 + i] = total;
+      if (reached) reached[i0 + i] = hcnt[i];
+    }
+  }
+  dawn::release(srcbuf);
+  return s;
+}
+
+dawn_status dawn_trace_enable(dawn_graph* g, int32_t enable) {
+  dawn::clear_error();
+  if (!g) {
+    dawn::set_error("graph is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  g->trace = enable != 0;
+  return DAWN_OK;
+}
+
+dawn_status dawn_trace_read(dawn_graph* g, dawn_trace_rec* out, int64_t cap, int64_t* count) {
+  dawn::clear_error();
+  if (!g || !count || cap < 0 || (cap > 0 && !out)) {
+    dawn::set_error("invalid trace_read arguments");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  const int64_t k = (int64_t)g->trace_log.size() < cap ? (int64_t)g->trace_log.size() : cap;
+  if (k > 0) std::memcpy(out, g->trace_log.data(), sizeof(dawn_trace_rec) * (size_t)k);
+  g->trace_log.erase(g->trace_log.begin(), g->trace_log.begin() + k);
+  *count = k;
+  return DAWN_OK;
+}
+
+}  // extern "C"

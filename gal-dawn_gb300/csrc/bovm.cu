@@ -1,0 +1,284 @@
+// Single-source boolean expand (BOVM) on sm_103a.
+//
+// Replaces the reference's SOVM kernel and its host level loop
+// (src/algorithm/gpu/bfs.cu:9-105).  The reference launches one thread per
+// vertex over all n rows every level, walks each row serially and polls a
+// racy flag from the host every third level.  Here a level is one of
+//   push: the compacted frontier queue is expanded warp-cooperatively; rows
+//         of >= 32 entries are swept by the whole warp with coalesced col
+//         loads, shorter rows are packed across lanes through a warp scan;
+//         a visited bitmap (L2-resident, n/8 bytes) is claimed with atomicOr;
+//   pull: every still-unvisited vertex scans its in-edges and stops at the
+//         first neighbour in the frontier bitmap (one warp owns 32 vertices,
+//         so bitmap words are written without atomics);
+// and a one-thread decide kernel picks the next level's direction (Beamer's
+// alpha/beta rule) on the device.  Both kernels emit the next frontier as a
+// queue and as a bitmap, so either direction can follow.  Distances are
+// written once, when a vertex is claimed.
+#include "dawn_device.cuh"
+
+namespace dawn {
+namespace {
+
+constexpr long long kAlpha = 14, kBeta = 24;
+
+__device__ __forceinline__ uint32_t* rot(uint32_t* fbm, int i, int nwords) {
+  return fbm + (size_t)(i % 3) * nwords;
+}
+
+// Fill the current source's distance row with -1 and clear the bitmaps.
+__global__ void __launch_bounds__(kBlock) bfs_clear(SsCtl* __restrict__ ctl, uint32_t* __restrict__ bitmaps,
+                                                    int32_t n, int32_t nwords) {
+  int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride) dist[i] = -1;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)4 * nwords; i += stride)
+    bitmaps[i] = 0;
+}
+
+__global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
+                         int32_t* __restrict__ q, uint32_t* __restrict__ vbm, int32_t n, long long m) {
+  if (threadIdx.x != 0) return;
+  const int32_t s = ctl->sources[ctl->src_idx];
+  int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
+  const int32_t deg = row_ptr[s + 1] - row_ptr[s];
+  ctl->source = s;
+  dist[s] = 0;
+  vbm[s >> 5] |= 1u << (s & 31);
+  q[0] = s;
+  ctl->qsize[0] = 1;
+  ctl->qsize[1] = 0;
+  ctl->mf[0] = (unsigned long long)deg;
+  ctl->mf[1] = 0;
+  ctl->mu = m - deg;
+  ctl->reached = (unsigned long long)deg;
+  ctl->level = 1;
+  ctl->mode = kModePush;
+  ctl->done = deg == 0;
+  ctl->prev_nf = 1;
+  ctl->n_push = 0;
+  ctl->n_pull = 0;
+}
+
+__global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ row_ptr,
+                                                   const int32_t* __restrict__ col, SsCtl* __restrict__ ctl,
+                                                   int32_t* __restrict__ q, uint32_t* __restrict__ vbm,
+                                                   uint32_t* __restrict__ fbm, int32_t n, int32_t nwords) {
+  __shared__ int s_excl[kBlock / 32][32];
+  __shared__ int s_rs[kBlock / 32][32];
+  __shared__ int s_v[kBlock / 32][32];
+  if (ctl->done || ctl->mode != kModePush) return;
+  const int L = ctl->level;
+  const int pin = (L - 1) & 1, pout = L & 1;
+  const int32_t* qin = q + (size_t)pin * n;
+  int32_t* qout = q + (size_t)pout * n;
+  uint32_t* fout = rot(fbm, L, nwords);
+  uint32_t* fclr = rot(fbm, L + 1, nwords);
+  int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
+  int32_t* qcount = &ctl->qsize[pout];
+  const int qn = ctl->qsize[pin];
+  const int lane = lane_id(), wib = threadIdx.x >> 5;
+
+  const size_t gstride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
+
+  unsigned long long my_mf = 0;
+  auto emit = [&](bool found, int32_t u) {
+    const int pos = warp_append(found, qcount);
+    if (found) {
+      qout[pos] = u;
+      dist[u] = L;
+      atomicOr(fout + (u >> 5), 1u << (u & 31));
+      my_mf += (unsigned long long)(row_ptr[u + 1] - row_ptr[u]);
+    }
+  };
+
+  warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], [&](int32_t, int k, bool valid) {
+    const int32_t u = valid ? __ldg(col + k) : -1;
+    const bool found = valid && claim_bit(vbm, u);
+    emit(found, u);
+  });
+  my_mf = warp_sum(my_mf);
+  if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
+}
+
+__global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ row_ptr,
+                                                   const int32_t* __restrict__ t_row_ptr,
+                                                   const int32_t* __restrict__ t_col, SsCtl* __restrict__ ctl,
+                                                   int32_t* __restrict__ q, uint32_t* __restrict__ vbm,
+                                                   uint32_t* __restrict__ fbm, int32_t n, int32_t nwords) {
+  if (ctl->done || ctl->mode != kModePull) return;
+  const int L = ctl->level;
+  const int pout = L & 1;
+  int32_t* qout = q + (size_t)pout * n;
+  const uint32_t* fin = rot(fbm, L - 1, nwords);
+  uint32_t* fout = rot(fbm, L, nwords);
+  uint32_t* fclr = rot(fbm, L + 1, nwords);
+  int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
+  int32_t* qcount = &ctl->qsize[pout];
+  const int lane = lane_id();
+
+  const size_t gstride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
+
+  unsigned long long my_mf = 0;
+  for (int w = global_warp(); w < nwords; w += num_warps()) {
+    const uint32_t vis = vbm[w];
+    uint32_t unv = ~vis;
+    if (w == nwords - 1 && (n & 31)) unv &= (1u << (n & 31)) - 1u;
+    if (unv == 0) continue;
+    const int32_t u = w * 32 + lane;
+    bool found = false;
+    if ((unv >> lane) & 1u) {
+      const int e = t_row_ptr[u + 1];
+      for (int k = t_row_ptr[u]; k < e; k++) {
+        if (test_bit(fin, __ldg(t_col + k))) {
+          found = true;
+          break;
+        }
+      }
+    }
+    const uint32_t fm = __ballot_sync(kFull, found);
+    if (fm) {
+      if (lane == 0) {
+        vbm[w] = vis | fm;
+        fout[w] = fm;
+      }
+      const int pos = warp_append(found, qcount);
+      if (found) {
+        qout[pos] = u;
+        dist[u] = L;
+        my_mf += (unsigned long long)(row_ptr[u + 1] - row_ptr[u]);
+      }
+    }
+  }
+  my_mf = warp_sum(my_mf);
+  if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
+}
+
+__global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop,
+                           int in_graph) {
+  if (threadIdx.x != 0) return;
+  if (ctl->done) {
+    if (in_graph) cudaGraphSetConditional(loop, 0);
+    return;
+  }
+  const int L = ctl->level, pout = L & 1;
+  const int nf = ctl->qsize[pout];
+  const unsigned long long mf = ctl->mf[pout];
+  ctl->reached += mf;
+  ctl->mu -= (long long)mf;
+  if (ctl->mode == kModePush) ctl->n_push++; else ctl->n_pull++;
+  if (nf == 0 || L >= n) {
+    ctl->done = 1;
+    if (in_graph) cudaGraphSetConditional(loop, 0);
+    return;
+  }
+  ctl->qsize[pout ^ 1] = 0;
+  ctl->mf[pout ^ 1] = 0;
+  int mode = ctl->mode;
+  if (ctl->policy == DAWN_VARIANT_DO) {
+    if (mode == kModePush) {
+      if ((long long)mf * kAlpha > ctl->mu && nf > ctl->prev_nf) mode = kModePull;
+    } else {
+      if ((long long)nf * kBeta < (long long)n && nf < ctl->prev_nf) mode = kModePush;
+    }
+  }
+  ctl->prev_nf = nf;
+  ctl->mode = mode;
+  ctl->level = L + 1;
+}
+
+__global__ void ss_next(SsCtl* __restrict__ ctl) {
+  if (threadIdx.x != 0) return;
+  ctl->total_reached += ctl->reached;
+  ctl->total_levels += ctl->level;
+  ctl->total_push += ctl->n_push;
+  ctl->total_pull += ctl->n_pull;
+  ctl->src_idx += 1;
+}
+
+void probe_ss(const void* p, LevelProbe* out) {
+  const SsCtl* c = static_cast<const SsCtl*>(p);
+  const int pin = (c->level - 1) & 1;
+  out->level = c->level;
+  out->mode = c->mode;
+  out->done = c->done;
+  out->frontier = c->qsize[pin];
+  out->frontier_edges = (int64_t)c->mf[pin];
+  out->unvisited_edges = c->mu;
+}
+
+}  // namespace
+
+dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,
+                       int32_t policy) {
+  const int32_t n = g->n;
+  int32_t nwords = (n + 31) / 32;
+  long long m = g->m;
+  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * (size_t)n));
+  DAWN_CHECK(ensure(g->ss_bitmaps, sizeof(uint32_t) * 4 * (size_t)nwords));
+  DAWN_CHECK(ensure(g->ss_ctl, sizeof(SsCtl)));
+  DAWN_CHECK(ensure(g->ss_sources, sizeof(int32_t) * (size_t)nsrc));
+  DAWN_CUDA(cudaMemcpyAsync(g->ss_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
+                            g->stream));
+  SsCtl c = {};
+  c.policy = policy;
+  c.nsrc = nsrc;
+  c.dist_base = d_dist;
+  c.sources = g->ss_sources.as<int32_t>();
+  DAWN_CHECK(upload_ctl(g, c));
+
+  struct {
+    SsCtl* ctl;
+    const int32_t *row_ptr, *col, *t_row_ptr, *t_col;
+    int32_t* q;
+    uint32_t *bitmaps, *vbm, *fbm;
+    int32_t n, nwords;
+    long long m;
+    cudaGraphConditionalHandle handle;
+    int in_graph;
+  } a;
+  a.ctl = g->ss_ctl.as<SsCtl>();
+  a.row_ptr = g->row_ptr;
+  a.col = g->col;
+  a.t_row_ptr = g->t_row_ptr;
+  a.t_col = g->t_col;
+  a.q = g->ss_queues.as<int32_t>();
+  a.bitmaps = g->ss_bitmaps.as<uint32_t>();
+  a.vbm = a.bitmaps;
+  a.fbm = a.bitmaps + nwords;
+  a.n = n;
+  a.nwords = nwords;
+  a.m = m;
+  a.handle = 0;
+  a.in_graph = 0;
+  void* clear_args[] = {&a.ctl, &a.bitmaps, &a.n, &a.nwords};
+  void* init_args[] = {&a.ctl, &a.row_ptr, &a.q, &a.vbm, &a.n, &a.m};
+  void* push_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.vbm, &a.fbm, &a.n, &a.nwords};
+  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.q, &a.vbm, &a.fbm, &a.n, &a.nwords};
+  void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
+  void* next_args[] = {&a.ctl};
+
+  const int sms = g->geo.sms;
+  SsFamily fam;
+  fam.npre = 2;
+  fam.pre[0] = {(const void*)bfs_clear, clear_args, dim3(sms * 4), dim3(kBlock)};
+  fam.pre[1] = {(const void*)bfs_init, init_args, dim3(1), dim3(32)};
+  fam.nbody = 3;
+  fam.body[0] = {(const void*)bfs_push, push_args, dim3(persistent_blocks((const void*)bfs_push, kBlock, 0)),
+                 dim3(kBlock), "bfs_push", kModePush};
+  fam.body[1] = {(const void*)bfs_pull, pull_args, dim3(persistent_blocks((const void*)bfs_pull, kBlock, 0)),
+                 dim3(kBlock), "bfs_pull", kModePull};
+  fam.body[2] = {(const void*)bfs_decide, decide_args, dim3(1), dim3(32), "bfs_decide"};
+  fam.post = {(const void*)ss_next, next_args, dim3(1), dim3(32), "ss_next"};
+  fam.ctl = a.ctl;
+  fam.ctl_bytes = sizeof(SsCtl);
+  fam.probe = probe_ss;
+  fam.handle = &a.handle;
+  fam.in_graph = &a.in_graph;
+  fam.done_flag = &a.ctl->done;
+  return ss_run(g, fam, nsrc, &g->bfs_exec);
+}
+
+}  // namespace dawn

@@ -1,0 +1,210 @@
+// Internal declarations shared by the translation units of libdawn_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <vector>
+
+#include "dawn_gb300.h"
+
+namespace dawn {
+
+void set_error(const char* fmt, ...);
+void clear_error();
+
+#define DAWN_CUDA(expr)                                                        \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      ::dawn::set_error("%s: %s (%s:%d)", #expr, cudaGetErrorString(e_),       \
+                        __FILE__, __LINE__);                                   \
+      return e_ == cudaErrorMemoryAllocation ? DAWN_ERR_OOM : DAWN_ERR_CUDA;   \
+    }                                                                          \
+  } while (0)
+
+#define DAWN_CHECK(expr)                                                       \
+  do {                                                                         \
+    dawn_status s_ = (expr);                                                   \
+    if (s_ != DAWN_OK) return s_;                                              \
+  } while (0)
+
+constexpr uint32_t kFull = 0xffffffffu;
+constexpr int kBlock = 256;  // threads per CTA of the frontier kernels
+
+// Device buffer owned by a graph handle; grows on demand, never shrinks.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+dawn_status ensure(DevBuf& b, size_t bytes);
+void release(DevBuf& b);
+
+// --- single-source frontier traversal (BOVM push/pull, GOVM push) ---------
+
+enum : int32_t { kModePush = 0, kModePull = 1 };
+
+// Device-resident control block of one single-source traversal.  Every
+// per-level kernel reads its parameters from here, so the same launches
+// (and the same captured CUDA graph) serve every level and every source.
+struct SsCtl {
+  int32_t qsize[2];             // frontier queue sizes by level parity
+  unsigned long long mf[2];     // out-degree sum of each queue
+  long long mu;                 // degree sum of still-unvisited vertices
+  unsigned long long reached;   // TEPS numerator of this source
+  int32_t level;                // level the next kernels compute
+  int32_t mode;                 // kModePush / kModePull for that level
+  int32_t done;                 // set when the frontier is empty
+  int32_t prev_nf;              // frontier size of the previous level
+  int32_t n_push, n_pull;       // per-source mode counters
+  int32_t src_idx;              // index into the source list
+  int32_t source;               // current source vertex
+  int32_t policy;               // DAWN_VARIANT_PUSH or DAWN_VARIANT_DO
+  int32_t weighted;             // GOVM: 0 int32, 1 float32 distances
+  int32_t err;                  // first device-side error code (0 = none)
+  int32_t nsrc;                 // sources of the current call
+  // per-call parameters (host-written before the first launch)
+  int32_t* dist_base;           // nsrc x n output, row src_idx is current
+  const int32_t* sources;       // device copy of the source list
+  // accumulated over all sources of the call
+  unsigned long long total_reached;
+  int32_t total_levels, total_push, total_pull, pad2;
+};
+
+// Kernel launches of one frontier-traversal family.  The driver runs them as
+// one CUDA graph per source (or per source batch):
+//   pre[0] -> ... -> while(cond){ body[0] -> ... -> body[nbody-1] } -> post
+// where the last body kernel ("decide") ends the loop through
+// cudaGraphSetConditional.  When conditional graphs are unavailable the
+// same sequence runs from a host loop that polls the `done` word.
+struct Launch {
+  const void* fn = nullptr;
+  void** args = nullptr;
+  dim3 grid, block;
+  const char* name = "";
+  int mode = -1;  // traced form: launch only at levels of this mode (-1 always)
+};
+
+// Frontier statistics a family exposes to the traced form (read from a
+// host copy of its control block before every level).
+struct LevelProbe {
+  int32_t level, mode, done;
+  int64_t frontier, frontier_edges, unvisited_edges;
+};
+struct SsFamily {
+  Launch pre[2];
+  int npre = 0;
+  Launch body[5];
+  int nbody = 0;
+  Launch post;
+  // the decide kernel (body[nbody-1]) takes these two arguments
+  cudaGraphConditionalHandle* handle = nullptr;
+  int* in_graph = nullptr;
+  // device address of the int32 `done` flag polled by the host loop
+  const void* done_flag = nullptr;
+  // traced form: the control block and how to read it
+  const void* ctl = nullptr;
+  size_t ctl_bytes = 0;
+  void (*probe)(const void* ctl, LevelProbe* out) = nullptr;
+};
+
+// Launch geometry for persistent grids on this device.
+struct Geometry {
+  int sms = 0;
+  int blocks_push = 0, blocks_pull = 0, blocks_relax = 0, blocks_bitset = 0;
+};
+
+}  // namespace dawn
+
+struct dawn_graph {
+  int device = 0;
+  int32_t n = 0;
+  int64_t m = 0;
+  uint32_t flags = 0;
+  dawn_wtype wtype = DAWN_W_NONE;
+  bool symmetric = false;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  dawn::Geometry geo;
+
+  // CSR (out-edges) and in-edge CSR for pull sweeps (aliases when symmetric)
+  int32_t* row_ptr = nullptr;
+  int32_t* col = nullptr;
+  void* val = nullptr;
+  int32_t* t_row_ptr = nullptr;
+  int32_t* t_col = nullptr;
+
+  // single-source workspace
+  dawn::DevBuf ss_queues;   // 2 x n int32
+  dawn::DevBuf ss_bitmaps;  // visited + 3 frontier bitmaps (words)
+  dawn::DevBuf ss_ctl;      // SsCtl
+  dawn::DevBuf ss_sources;  // int32 source list of the current call
+  dawn::DevBuf ss_scratch;  // n x u64 (GOVM source-row resolution)
+  dawn::SsCtl* h_ctl = nullptr;  // pinned: [0] upload staging, [1] download
+  bool graphs_ok = true;         // conditional CUDA graphs usable
+
+  // batched bitset workspace
+  dawn::DevBuf bs_words;    // visit / frontier / next words
+  dawn::DevBuf bs_queues;   // active + touched queues
+  dawn::DevBuf bs_ctl;
+  dawn::DevBuf bs_sources;
+
+  // closeness reduction
+  dawn::DevBuf cc_out;
+
+  // distance staging for host-pointer calls
+  dawn::DevBuf dist_stage;
+
+  // captured single-source traversal graphs (one per kernel family)
+  cudaGraphExec_t bfs_exec = nullptr;
+  cudaGraphExec_t sssp_exec = nullptr;
+  int32_t sssp_exec_weighted = -1;
+  cudaGraphExec_t bs_exec = nullptr;
+
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+
+  // per-level trace (dawn_trace_enable)
+  bool trace = false;
+  std::vector<dawn_trace_rec> trace_log;
+  cudaEvent_t trace_ev[10] = {};
+};
+
+namespace dawn {
+
+// bovm.cu
+dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,
+                       int32_t* d_dist, int32_t policy);
+// msbfs.cu
+dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc,
+                       int32_t* d_dist);
+dawn_status bfs_bitset_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc);
+// govm.cu
+dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,
+                        void* d_dist);
+// runtime.cu
+dawn_status ss_run(dawn_graph* g, SsFamily& fam, int32_t nsrc,
+                   cudaGraphExec_t* exec_cache);
+dawn_status upload_ctl(dawn_graph* g, const SsCtl& c);
+dawn_status download_ctl(dawn_graph* g, SsCtl* out);
+int persistent_blocks(const void* fn, int block, size_t smem);
+dawn_status build_transpose(dawn_graph* g);
+// Per-row reductions over a distance block (kind 0 hops, 1 int32, 2 float):
+// with degree = 0, d_sum gets the exact sum of reached distances of v != s
+// (int64 bits for kinds 0/1, float64 for kind 2) and d_cnt their count;
+// with degree = 1, d_sum gets (int64 bits) the out-degree sum of the
+// reached vertices, source included: the TEPS numerator.
+dawn_status row_reduce(dawn_graph* g, const void* d_dist, int32_t nsrc,
+                       const int32_t* d_sources, int kind, int degree,
+                       double* d_sum, long long* d_cnt);
+const char* last_error();
+dawn_status validate_csr(dawn_graph* g);
+dawn_status exclusive_scan_i64(const int64_t* d_in, int64_t* d_out, int64_t n,
+                               cudaStream_t s);
+
+}  // namespace dawn

@@ -1,0 +1,236 @@
+"""ctypes bindings of the C ABI in include/dawn_gb300.h (libdawn_gb300.so).
+
+There is no fallback: the compute is the CUDA library.  A missing library
+or a failing call raises :class:`DawnError` with the library's message.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import LIB_DIR
+
+OK, ERR_INVALID_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = 0, 1, 2, 3, 4, 5
+W_NONE, W_I32, W_F32 = 0, 1, 2
+GRAPH_SYMMETRIC, GRAPH_NO_VALIDATE = 1, 2
+VARIANT_AUTO, VARIANT_PUSH, VARIANT_DO, VARIANT_BITSET, VARIANT_LEARNED = 0, 1, 2, 3, 4
+INT32_MAX = np.iinfo(np.int32).max
+FLT_MAX = np.float32(3.4028235e38)
+
+LIB_PATH = os.path.join(LIB_DIR, "libdawn_gb300.so")
+
+# Every symbol the header declares; tests check the library exports them.
+EXPORTS = ("dawn_graph_create", "dawn_graph_create_device", "dawn_graph_destroy",
+           "dawn_graph_set_stream", "dawn_graph_synchronize", "dawn_bfs", "dawn_bfs_device",
+           "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_trace_enable", "dawn_trace_read",
+           "dawn_last_error", "dawn_version")
+
+
+class DawnError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"dawn status {status}: {msg}")
+        self.status = status
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("edges_traversed", ctypes.c_int64), ("levels", ctypes.c_int32),
+                ("push_levels", ctypes.c_int32), ("pull_levels", ctypes.c_int32),
+                ("batches", ctypes.c_int32), ("device_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+    def __repr__(self):
+        return "Stats(" + ", ".join(f"{k}={v}" for k, v in self.as_dict().items()) + ")"
+
+
+class TraceRec(ctypes.Structure):
+    _fields_ = [("kernel", ctypes.c_char * 24), ("run", ctypes.c_int32), ("level", ctypes.c_int32),
+                ("mode", ctypes.c_int32), ("pad", ctypes.c_int32), ("frontier", ctypes.c_int64),
+                ("frontier_edges", ctypes.c_int64), ("unvisited_edges", ctypes.c_int64),
+                ("ms", ctypes.c_float), ("pad2", ctypes.c_float)]
+
+
+_lib = None
+_VP = ctypes.c_void_p
+_I32P = ctypes.POINTER(ctypes.c_int32)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise DawnError(ERR_UNSUPPORTED, f"{LIB_PATH} missing: run __graft_entry__.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        L.dawn_graph_create.argtypes = [_VP, _VP, _VP, ctypes.c_int, ctypes.c_int32, ctypes.c_int64,
+                                        ctypes.c_uint32, _VP, ctypes.POINTER(_VP)]
+        L.dawn_graph_create_device.argtypes = L.dawn_graph_create.argtypes
+        L.dawn_graph_destroy.argtypes = [_VP]
+        L.dawn_graph_set_stream.argtypes = [_VP, _VP]
+        L.dawn_graph_synchronize.argtypes = [_VP]
+        L.dawn_bfs.argtypes = [_VP, _VP, ctypes.c_int32, _VP, ctypes.c_int32, ctypes.POINTER(Stats)]
+        L.dawn_bfs_device.argtypes = L.dawn_bfs.argtypes
+        L.dawn_sssp.argtypes = L.dawn_bfs.argtypes
+        L.dawn_sssp_device.argtypes = L.dawn_bfs.argtypes
+        L.dawn_closeness.argtypes = [_VP, _VP, ctypes.c_int32, ctypes.c_int32, _VP, _VP, _VP,
+                                     ctypes.POINTER(Stats)]
+        L.dawn_trace_enable.argtypes = [_VP, ctypes.c_int32]
+        L.dawn_trace_read.argtypes = [_VP, ctypes.POINTER(TraceRec), ctypes.c_int64,
+                                      ctypes.POINTER(ctypes.c_int64)]
+        for f in EXPORTS:
+            getattr(L, f).restype = ctypes.c_int32
+        L.dawn_last_error.restype = ctypes.c_char_p
+        L.dawn_last_error.argtypes = []
+        L.dawn_version.restype = ctypes.c_char_p
+        L.dawn_version.argtypes = []
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != OK:
+        raise DawnError(rc, lib().dawn_last_error().decode(errors="replace"))
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Graph:
+    """A CSR graph resident on the current CUDA device.
+
+    ``g`` is any object with ``n``, ``row_ptr``, ``col`` and optional
+    ``w_i32`` / ``w_f32`` / ``symmetric`` attributes (e.g. gen.CsrGraph).
+    ``weights`` selects "i32", "f32" or None (unweighted).
+    """
+
+    def __init__(self, g=None, weights=None, symmetric=None, stream=None, validate=True, raw=None):
+        if raw is not None:
+            self._init_raw(**raw)
+            return
+        self.n = int(g.n)
+        self._rp = np.ascontiguousarray(g.row_ptr, np.int32)
+        self._col = np.ascontiguousarray(g.col, np.int32)
+        self.m = int(self._col.shape[0])
+        self.wtype = {None: W_NONE, "i32": W_I32, "f32": W_F32}[weights]
+        self._val = None
+        if self.wtype == W_I32:
+            self._val = np.ascontiguousarray(g.w_i32, np.int32)
+        elif self.wtype == W_F32:
+            self._val = np.ascontiguousarray(g.w_f32, np.float32)
+        sym = bool(getattr(g, "symmetric", False)) if symmetric is None else bool(symmetric)
+        flags = (GRAPH_SYMMETRIC if sym else 0) | (0 if validate else GRAPH_NO_VALIDATE)
+        h = ctypes.c_void_p()
+        _check(lib().dawn_graph_create(_ptr(self._rp), _ptr(self._col), _ptr(self._val), self.wtype,
+                                       self.n, self.m, flags, ctypes.c_void_p(stream or 0),
+                                       ctypes.byref(h)))
+        self.handle = h
+        self.degrees = np.diff(self._rp.astype(np.int64))
+
+    def _init_raw(self, n, m, row_ptr, col, val=0, wtype=W_NONE, symmetric=False, stream=None,
+                  validate=True, device=False):
+        """Create from raw pointers (host, or device when device=True)."""
+        self.n, self.m, self.wtype = int(n), int(m), wtype
+        self._rp = self._col = self._val = None
+        flags = (GRAPH_SYMMETRIC if symmetric else 0) | (0 if validate else GRAPH_NO_VALIDATE)
+        h = ctypes.c_void_p()
+        fn = lib().dawn_graph_create_device if device else lib().dawn_graph_create
+        _check(fn(ctypes.c_void_p(row_ptr), ctypes.c_void_p(col), ctypes.c_void_p(val or 0), wtype, self.n,
+                  self.m, flags, ctypes.c_void_p(stream or 0), ctypes.byref(h)))
+        self.handle = h
+        self.degrees = None
+
+    def bfs_host_ptr(self, sources, dist_ptr, variant=VARIANT_AUTO):
+        """dawn_bfs into a caller host buffer (e.g. pinned memory)."""
+        s = np.ascontiguousarray(sources, np.int32)
+        st = Stats()
+        _check(lib().dawn_bfs(self.handle, _ptr(s), len(s), ctypes.c_void_p(dist_ptr), variant,
+                              ctypes.byref(st)))
+        return st
+
+    # -- lifetime --
+    def close(self):
+        if self.handle:
+            _check(lib().dawn_graph_destroy(self.handle))
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        _check(lib().dawn_graph_set_stream(self.handle, ctypes.c_void_p(stream or 0)))
+
+    def synchronize(self):
+        _check(lib().dawn_graph_synchronize(self.handle))
+
+    def trace(self, enable=True):
+        _check(lib().dawn_trace_enable(self.handle, int(enable)))
+
+    def trace_read(self):
+        """All pending per-level records as a list of dicts."""
+        out = []
+        buf = (TraceRec * 4096)()
+        while True:
+            cnt = ctypes.c_int64()
+            _check(lib().dawn_trace_read(self.handle, buf, 4096, ctypes.byref(cnt)))
+            for r in buf[:cnt.value]:
+                out.append({"kernel": r.kernel.decode(), "run": r.run, "level": r.level, "mode": r.mode,
+                            "frontier": r.frontier, "frontier_edges": r.frontier_edges,
+                            "unvisited_edges": r.unvisited_edges, "ms": r.ms})
+            if cnt.value < 4096:
+                return out
+
+    # -- traversals (host buffers) --
+    def bfs(self, sources, variant=VARIANT_AUTO, out=None):
+        s = np.ascontiguousarray(sources, np.int32)
+        d = out if out is not None else np.empty((len(s), self.n), np.int32)
+        st = Stats()
+        _check(lib().dawn_bfs(self.handle, _ptr(s), len(s), _ptr(d), variant, ctypes.byref(st)))
+        return d, st
+
+    def sssp(self, sources, out=None):
+        s = np.ascontiguousarray(sources, np.int32)
+        dt = np.float32 if self.wtype == W_F32 else np.int32
+        d = out if out is not None else np.empty((len(s), self.n), dt)
+        st = Stats()
+        _check(lib().dawn_sssp(self.handle, _ptr(s), len(s), _ptr(d), 0, ctypes.byref(st)))
+        return d, st
+
+    def closeness(self, sources, weighted=False):
+        s = np.ascontiguousarray(sources, np.int32)
+        cc = np.empty(len(s), np.float64)
+        sums = np.empty(len(s), np.float64)
+        reached = np.empty(len(s), np.int64)
+        st = Stats()
+        _check(lib().dawn_closeness(self.handle, _ptr(s), len(s), int(weighted), _ptr(cc), _ptr(sums),
+                                    _ptr(reached), ctypes.byref(st)))
+        return cc, sums, reached
+
+    # -- traversals (device buffers, e.g. torch tensors' data_ptr()) --
+    def bfs_device(self, sources, d_dist, variant=VARIANT_AUTO, stats=True):
+        s = np.ascontiguousarray(sources, np.int32)
+        st = Stats() if stats else None
+        _check(lib().dawn_bfs_device(self.handle, _ptr(s), len(s), ctypes.c_void_p(d_dist), variant,
+                                     ctypes.byref(st) if st is not None else None))
+        return st
+
+    def sssp_device(self, sources, d_dist, stats=True):
+        s = np.ascontiguousarray(sources, np.int32)
+        st = Stats() if stats else None
+        _check(lib().dawn_sssp_device(self.handle, _ptr(s), len(s), ctypes.c_void_p(d_dist), 0,
+                                      ctypes.byref(st) if st is not None else None))
+        return st
+
+
+def version():
+    return lib().dawn_version().decode()

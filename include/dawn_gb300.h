@@ -1,0 +1,174 @@
+/* dawn_gb300.h — C ABI of the GB300-native DAWN frontier path.
+ *
+ * These entry points replace the device side of GAL-DAWN's GPU algorithms.
+ * They take plain pointers and sizes (no C++ or torch types), return a
+ * status code on every call and keep device state behind an opaque graph
+ * handle.  Citations are to the reference project's files.
+ *
+ * Encodings
+ *   hop distance   int32, -1 = unreachable, 0 = the source itself.  The
+ *                  reference stores 0 for both (src/algorithm/cpu/bfs.cpp:62);
+ *                  the C++ host layer converts back for its text output.
+ *   int32 weights  int32 distance, INT32_MAX = unreachable.
+ *   float weights  float distance, FLT_MAX = unreachable, as the reference
+ *                  (src/algorithm/cpu/sssp.cpp:36).
+ *   dist arrays    row-major nsrc x n: row i belongs to sources[i].
+ *
+ * Threading: a graph handle is not thread safe; calls on one handle are
+ * ordered on its CUDA stream.  Different handles may be used concurrently.
+ */
+#ifndef DAWN_GB300_H
+#define DAWN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t dawn_status;
+#define DAWN_OK 0
+#define DAWN_ERR_INVALID_ARG 1 /* bad pointer, size, CSR or source id */
+#define DAWN_ERR_OOM 2         /* device allocation failed */
+#define DAWN_ERR_CUDA 3        /* a CUDA runtime call failed */
+#define DAWN_ERR_TIMEOUT 4     /* a bounded device wait gave up */
+#define DAWN_ERR_UNSUPPORTED 5 /* variant / weight type not available */
+
+typedef enum dawn_wtype {
+  DAWN_W_NONE = 0, /* unweighted */
+  DAWN_W_I32 = 1,  /* int32 edge weights */
+  DAWN_W_F32 = 2   /* float32 edge weights (non-negative) */
+} dawn_wtype;
+
+/* dawn_graph_create flags */
+#define DAWN_GRAPH_SYMMETRIC 1u   /* every edge is stored in both directions */
+#define DAWN_GRAPH_NO_VALIDATE 2u /* skip the O(n + m) CSR validation pass */
+
+/* Traversal variants (the result never depends on the variant). */
+#define DAWN_VARIANT_AUTO 0    /* library choice: BITSET for >= 2 sources */
+#define DAWN_VARIANT_PUSH 1    /* single source, top-down queue every level */
+#define DAWN_VARIANT_DO 2      /* single source, push/pull by heuristic */
+#define DAWN_VARIANT_BITSET 3  /* batched: 64 sources per uint64 frontier word */
+#define DAWN_VARIANT_LEARNED 4 /* batched, per-level kernel chosen by the MLP */
+
+typedef struct dawn_stats {
+  int64_t edges_traversed; /* TEPS numerator: sum over sources of the CSR
+                              entries whose tail vertex was reached */
+  int32_t levels;          /* frontier iterations, summed over batches */
+  int32_t push_levels;     /* iterations that ran a push (top-down) kernel */
+  int32_t pull_levels;     /* iterations that ran a pull (bottom-up) kernel */
+  int32_t batches;         /* source batches (single-source: = nsrc) */
+  float device_ms;         /* CUDA-event time of the traversal only */
+} dawn_stats;
+
+typedef struct dawn_graph dawn_graph;
+
+/* Uploads a host CSR (row_ptr[n+1], col[m], optional val[m]) to the current
+ * CUDA device.  Replaces the per-call thrust::copy_n of the CSR in
+ * BFS_GPU::run (src/algorithm/gpu/bfs.cu:115-118), SSSP_GPU::run
+ * (src/algorithm/gpu/sssp.cu:139-144) and MSSP_GPU::run
+ * (src/algorithm/gpu/mssp.cu:14-17, 58-63): the graph stays resident for
+ * any number of traversals.  stream may be NULL (library-owned stream). */
+dawn_status dawn_graph_create(const int32_t* row_ptr, const int32_t* col,
+                              const void* val, dawn_wtype wtype, int32_t n,
+                              int64_t m, uint32_t flags, void* stream,
+                              dawn_graph** out);
+
+/* As dawn_graph_create, from device-resident arrays (copied device to
+ * device; the caller keeps ownership of its buffers). */
+dawn_status dawn_graph_create_device(const int32_t* d_row_ptr,
+                                     const int32_t* d_col, const void* d_val,
+                                     dawn_wtype wtype, int32_t n, int64_t m,
+                                     uint32_t flags, void* stream,
+                                     dawn_graph** out);
+
+/* Frees every device buffer of the handle.  Replaces the thrust
+ * device_vector destructors at the end of each reference run(). */
+dawn_status dawn_graph_destroy(dawn_graph* g);
+
+/* Sets the CUDA stream later calls are ordered on (NULL = library stream). */
+dawn_status dawn_graph_set_stream(dawn_graph* g, void* stream);
+
+/* Waits for the handle's stream. */
+dawn_status dawn_graph_synchronize(dawn_graph* g);
+
+/* Hop distances from nsrc sources (host arrays; dist is nsrc x n int32).
+ * Replaces BFS_GPU::kernel + SOVM (src/algorithm/gpu/bfs.cu:9-105) for one
+ * source, and the per-source loops of MSSP_GPU::run
+ * (src/algorithm/gpu/mssp.cu:9-51) and APSP_GPU::run
+ * (src/algorithm/gpu/apsp.cu:62-111) for many.  Sources must lie in [0, n);
+ * isolated sources are legal (their row holds only the 0 at the source).
+ * stats may be NULL. */
+dawn_status dawn_bfs(dawn_graph* g, const int32_t* sources, int32_t nsrc,
+                     int32_t* dist, int32_t variant, dawn_stats* stats);
+
+/* As dawn_bfs with dist in device memory (nsrc x n).  Asynchronous on the
+ * handle's stream when stats is NULL. */
+dawn_status dawn_bfs_device(dawn_graph* g, const int32_t* sources,
+                            int32_t nsrc, int32_t* d_dist, int32_t variant,
+                            dawn_stats* stats);
+
+/* Weighted shortest-path distances (min-plus relax).  dist is nsrc x n of
+ * int32 (DAWN_W_I32 graphs) or float (DAWN_W_F32 graphs).  Replaces
+ * SSSP_GPU::kernel + GOVM (src/algorithm/gpu/sssp.cu:18-129) and
+ * MSSP_GPU::run_Weighted (src/algorithm/gpu/mssp.cu:53-102).  The source's
+ * own row initialises its neighbours with the last CSR entry of a repeated
+ * neighbour, as the reference CPU path does (src/algorithm/cpu/sssp.cpp:41-45). */
+dawn_status dawn_sssp(dawn_graph* g, const int32_t* sources, int32_t nsrc,
+                      void* dist, int32_t variant, dawn_stats* stats);
+dawn_status dawn_sssp_device(dawn_graph* g, const int32_t* sources,
+                             int32_t nsrc, void* d_dist, int32_t variant,
+                             dawn_stats* stats);
+
+/* Closeness centrality of each source, (n - 1) / sum of d(s, v) over the
+ * reached v != s, accumulated exactly (int64 for hops and int32 weights,
+ * float64 for float weights) and divided in float64.  weighted = 0 uses hop
+ * distances, 1 the graph's weights.  dist_sum / reached (nullable) return
+ * the sum and the number of reached vertices other than s, from which the
+ * reference's own integer-division value (src/algorithm/cpu/cc.cpp:77-78,
+ * src/algorithm/gpu/cc.cu:92-94) can be recomputed.  Replaces
+ * CC_GPU::kernel / kernel_Weighted (src/algorithm/gpu/cc.cu:32-202). */
+dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources,
+                           int32_t nsrc, int32_t weighted, double* cc,
+                           double* dist_sum, int64_t* reached,
+                           dawn_stats* stats);
+
+/* Per-level trace.  No counterpart in the reference, which only times whole
+ * runs with host std::chrono (src/algorithm/gpu/bfs.cu:70,93-95).  While
+ * tracing is enabled on a handle, traversals run level by level from the
+ * host instead of as one CUDA graph per source batch: before each level the
+ * host reads the frontier statistics, launches only the kernels that level
+ * uses, brackets each with CUDA events on the handle's stream, and appends
+ * one record per kernel.  Results are identical; only speed differs.  The
+ * records are the per-iteration timing log the variant selector trains on
+ * and the per-kernel durations the roofline report divides by. */
+typedef struct dawn_trace_rec {
+  char kernel[24];          /* kernel name */
+  int32_t run;              /* source index (single-source) or batch index */
+  int32_t level;            /* 1-based frontier iteration */
+  int32_t mode;             /* 0 push (top-down), 1 pull (bottom-up) */
+  int32_t pad;
+  int64_t frontier;         /* vertices in the frontier entering the level */
+  int64_t frontier_edges;   /* out-degree sum of that frontier */
+  int64_t unvisited_edges;  /* degree sum of vertices not yet finished */
+  float ms;                 /* CUDA-event duration of the kernel */
+  float pad2;
+} dawn_trace_rec;
+
+dawn_status dawn_trace_enable(dawn_graph* g, int32_t enable);
+/* Copies up to cap records (oldest first) and removes them from the handle;
+ * *count receives the number copied. */
+dawn_status dawn_trace_read(dawn_graph* g, dawn_trace_rec* out, int64_t cap,
+                            int64_t* count);
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char* dawn_last_error(void);
+
+/* Library version string. */
+const char* dawn_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DAWN_GB300_H */

@@ -1,0 +1,102 @@
+"""Hop distances through the C ABI against the oracle (bit-exact)."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from dawn_gb300 import abi, gen
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = [abi.VARIANT_PUSH, abi.VARIANT_DO, abi.VARIANT_BITSET, abi.VARIANT_AUTO]
+
+
+def expected(g, srcs):
+    ref, edges, _ = O.mssp(g, srcs)
+    return O.hops_ref_to_api(ref, srcs), edges
+
+
+def check(g, srcs, variants=VARIANTS, symmetric=None):
+    want, edges = expected(g, srcs)
+    with abi.Graph(g, symmetric=symmetric) as dg:
+        for v in variants:
+            d, st = dg.bfs(srcs, variant=v)
+            bad = np.argwhere(d != want)
+            assert bad.size == 0, (v, bad[:5], d[tuple(bad[0])], want[tuple(bad[0])])
+            assert st.edges_traversed == edges, (v, st.edges_traversed, edges)
+
+
+def test_golden(goldens):
+    for g in goldens:
+        check(g, g.sources)
+        want = O.hops_ref_to_api(g.bfs_ref, g.sources)
+        with abi.Graph(g) as dg:
+            d, _ = dg.bfs(g.sources)
+            assert np.array_equal(d, want), g.name
+
+
+def test_directed_er_64k():
+    # The CPU-runnable workload: directed ER, n = 65,536, 2^20 edges drawn.
+    g = gen.erdos_renyi(65536, 1 << 20, seed=1)
+    check(g, gen.sources(g, 64, seed=2, from_lcc=False))
+
+
+@pytest.mark.parametrize("nsrc", [1, 2, 63, 64, 65, 130])
+def test_rmat_batch_boundaries(nsrc):
+    g = gen.rmat(14, 16, seed=3)
+    srcs = gen.sources(g, nsrc, seed=nsrc)
+    check(g, srcs, variants=[abi.VARIANT_BITSET, abi.VARIANT_DO])
+
+
+def test_duplicate_and_isolated_sources():
+    g = gen.rmat(12, 4, seed=4)
+    iso = np.nonzero(g.degrees() == 0)[0]
+    assert len(iso) > 0
+    s = gen.sources(g, 10, seed=5)
+    srcs = np.concatenate([s[:5], s[:3], iso[:2], s[5:]]).astype(np.int32)
+    check(g, srcs)
+
+
+def test_high_diameter_grid():
+    g = gen.grid(60, 170)
+    check(g, np.array([0, 60 * 170 - 1, 5000], np.int32))
+
+
+def test_knn():
+    g = gen.knn(20000, 8, seed=6)
+    check(g, gen.sources(g, 40, seed=7))
+
+
+def test_unsorted_rows_self_loops_duplicates():
+    rng = np.random.default_rng(8)
+    n = 3000
+    src = rng.integers(0, n, 40000)
+    dst = rng.integers(0, n, 40000)
+    dst[:500] = src[:500]
+    order = np.argsort(src, kind="stable")  # rows grouped, columns unsorted
+    g = gen.CsrGraph(n, np.concatenate([[0], np.cumsum(np.bincount(src, minlength=n))]).astype(np.int32),
+                     dst[order].astype(np.int32))
+    check(g, np.arange(0, n, 97, dtype=np.int32))
+
+
+def test_single_vertex_and_edgeless():
+    g1 = gen.CsrGraph(1, np.array([0, 0], np.int32), np.zeros(0, np.int32))
+    with abi.Graph(g1) as dg:
+        for v in VARIANTS:
+            d, st = dg.bfs([0, 0], variant=v)
+            assert d.tolist() == [[0], [0]] and st.edges_traversed == 0
+    g2 = gen.CsrGraph(70, np.zeros(71, np.int32), np.zeros(0, np.int32))
+    with abi.Graph(g2) as dg:
+        d, _ = dg.bfs(np.arange(70, dtype=np.int32), variant=abi.VARIANT_BITSET)
+        assert np.array_equal(d, np.where(np.eye(70, dtype=bool), 0, -1))
+
+
+def test_repeated_calls_reuse_graph():
+    g = gen.rmat(13, 8, seed=9)
+    srcs = gen.sources(g, 100, seed=10)
+    want, _ = expected(g, srcs)
+    with abi.Graph(g) as dg:
+        for _ in range(3):
+            for v in (abi.VARIANT_BITSET, abi.VARIANT_DO):
+                d, _ = dg.bfs(srcs, variant=v)
+                assert np.array_equal(d, want)

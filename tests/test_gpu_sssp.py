@@ -1,0 +1,84 @@
+"""Weighted distances (min-plus relax) through the C ABI against the oracle."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from dawn_gb300 import abi, gen
+
+pytestmark = pytest.mark.gpu
+
+
+def to_ref(d):
+    """C-ABI int32 distances -> the reference's float encoding (FLT_MAX)."""
+    if d.dtype == np.float32:
+        return d
+    return np.where(d == abi.INT32_MAX, abi.FLT_MAX, d.astype(np.float32))
+
+
+def check(g, srcs, weights=("i32", "f32")):
+    want = O.msssp(g, srcs)
+    for w in weights:
+        with abi.Graph(g, weights=w) as dg:
+            d, st = dg.sssp(srcs)
+            got = to_ref(d)
+            bad = np.argwhere(got != want)
+            assert bad.size == 0, (w, bad[:5])
+            reached = want != abi.FLT_MAX
+            assert st.edges_traversed == int((reached * g.degrees()[None, :]).sum())
+
+
+def test_golden(goldens):
+    for g in goldens:
+        if g.sssp_ref is None:
+            continue
+        check(g, g.sources)
+        with abi.Graph(g, weights="f32") as dg:
+            d, _ = dg.sssp(g.sources)
+        d[d == 0] = 0
+        assert np.array_equal(d, g.sssp_ref), g.name
+
+
+def test_directed_er():
+    g = gen.erdos_renyi(20000, 200000, seed=11, weights=True)
+    check(g, gen.sources(g, 8, seed=12, from_lcc=False))
+
+
+def test_rmat():
+    g = gen.rmat(14, 16, seed=13, weights=True)
+    check(g, gen.sources(g, 8, seed=14))
+
+
+def test_grid_high_diameter():
+    g = gen.grid(50, 90, seed=15, weights=True)
+    check(g, np.array([0, 2222, 4499], np.int32))
+
+
+def test_source_row_duplicates_last_wins():
+    # 0->1 twice (3 then 5), 1->2 (1), 0->0 absent: the reference keeps 5.
+    rp = np.array([0, 2, 3, 3], np.int32)
+    col = np.array([1, 1, 2], np.int32)
+    g = gen.CsrGraph(3, rp, col, np.array([3, 5, 1], np.int32), np.array([3, 5, 1], np.float32))
+    want = O.msssp(g, [0])
+    assert want.tolist() == [[0.0, 5.0, 6.0]]
+    check(g, [0])
+
+
+def test_source_self_loop_is_expanded():
+    # With a self loop the source enters the first frontier (alpha[source]),
+    # so the shorter duplicate is found through it.
+    rp = np.array([0, 3, 4, 4], np.int32)
+    col = np.array([0, 1, 1, 2], np.int32)
+    w = np.array([7, 3, 5, 1], np.int32)
+    g = gen.CsrGraph(3, rp, col, w, w.astype(np.float32))
+    want = O.msssp(g, [0])
+    assert want.tolist() == [[0.0, 3.0, 4.0]]
+    check(g, [0])
+
+
+def test_unweighted_graph_rejected():
+    g = gen.rmat(8, 4, seed=1)
+    with abi.Graph(g) as dg:
+        with pytest.raises(abi.DawnError) as e:
+            dg.sssp([0])
+        assert e.value.status == abi.ERR_UNSUPPORTED
