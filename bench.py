@@ -140,6 +140,10 @@ def bitset_roofline(dg, g, srcs, d_dist, abi, peak_gbs, peak_kind):
     dg.synchronize()
     recs = dg.trace_read()
     dg.trace(False)
+    for r in recs:
+        log("[trace] run %d level %d mode %d %-16s frontier %9d fedges %11d unfinished_edges %11d  %.3f ms" % (
+            r["run"], r["level"], r["mode"], r["kernel"], r["frontier"], r["frontier_edges"],
+            r["unvisited_edges"], r["ms"]))
     per = {}
     for r in recs:
         k = per.setdefault(r["kernel"], {"launches": 0, "ms": 0.0, "bytes": 0})
@@ -271,7 +275,12 @@ def main():
         dist.init_process_group("nccl")
         barrier = dist.barrier
     g, srcs = make_workload(args.scale, rank)
-    stream = torch.cuda.current_stream().cuda_stream
+    # A dedicated stream: the library launches on it and torch's events
+    # record on it (the legacy default stream has handle 0, which the C ABI
+    # reads as "library-owned stream").
+    tstream = torch.cuda.Stream()
+    torch.cuda.set_stream(tstream)
+    stream = tstream.cuda_stream
     peak_gbs, peak_kind = peaks()
 
     dg = abi.Graph(g, stream=stream)
@@ -298,6 +307,15 @@ def main():
     plain = {"value": round(edges / (ms_plain * 1e-3) / 1e9, 3), "unit": "GTEPS",
              "ms_per_step": round(ms_plain, 3), "variant": "single-source push/pull (direction-optimising)"}
 
+    if os.environ.get("DAWN_BENCH_TRACE_PLAIN"):
+        dg.trace(True)
+        dg.bfs_device(srcs[:2], d_dist.data_ptr(), variant=abi.VARIANT_DO, stats=False)
+        dg.synchronize()
+        for r in dg.trace_read():
+            log("[trace-plain] src %d level %d mode %d %-10s frontier %9d fedges %11d unvisited_edges %11d %.3f ms"
+                % (r["run"], r["level"], r["mode"], r["kernel"], r["frontier"], r["frontier_edges"],
+                   r["unvisited_edges"], r["ms"]))
+        dg.trace(False)
     roof, recs = bitset_roofline(dg, g, srcs, d_dist.data_ptr(), abi, peak_gbs, peak_kind)
     step_bytes = 4 * g.m + 4 * (g.n + 1) + NSRC * 4 * g.n
     roof["step_alg_bytes"] = step_bytes

@@ -45,9 +45,12 @@ __global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ ro
   ctl->source = s;
   dist[s] = 0;
   vbm[s >> 5] |= 1u << (s & 31);
-  q[0] = s;
-  ctl->qsize[0] = 1;
+  const bool is_long = deg >= kLongRow;
+  q[(is_long ? 2 : 0) * (size_t)n] = s;
+  ctl->qsize[0] = is_long ? 0 : 1;
+  ctl->lsize[0] = is_long ? 1 : 0;
   ctl->qsize[1] = 0;
+  ctl->lsize[1] = 0;
   ctl->mf[0] = (unsigned long long)deg;
   ctl->mf[1] = 0;
   ctl->mu = m - deg;
@@ -67,37 +70,40 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
+  __shared__ LongTile s_long;
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
   const int32_t* qin = q + (size_t)pin * n;
+  const int32_t* qlin = q + (size_t)(2 + pin) * n;
   int32_t* qout = q + (size_t)pout * n;
+  int32_t* qlout = q + (size_t)(2 + pout) * n;
   uint32_t* fout = rot(fbm, L, nwords);
   uint32_t* fclr = rot(fbm, L + 1, nwords);
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
   int32_t* qcount = &ctl->qsize[pout];
-  const int qn = ctl->qsize[pin];
+  int32_t* lcount = &ctl->lsize[pout];
+  const int qn = ctl->qsize[pin], ln = ctl->lsize[pin];
   const int lane = lane_id(), wib = threadIdx.x >> 5;
 
   const size_t gstride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
 
   unsigned long long my_mf = 0;
-  auto emit = [&](bool found, int32_t u) {
-    const int pos = warp_append(found, qcount);
-    if (found) {
-      qout[pos] = u;
-      dist[u] = L;
-      atomicOr(fout + (u >> 5), 1u << (u & 31));
-      my_mf += (unsigned long long)(row_ptr[u + 1] - row_ptr[u]);
-    }
-  };
-
-  warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], [&](int32_t, int k, bool valid) {
+  auto op = [&](int32_t, int k, bool valid) {
     const int32_t u = valid ? __ldg(col + k) : -1;
     const bool found = valid && claim_bit(vbm, u);
-    emit(found, u);
-  });
+    int deg = 0;
+    if (found) {
+      deg = row_ptr[u + 1] - row_ptr[u];
+      dist[u] = L;
+      atomicOr(fout + (u >> 5), 1u << (u & 31));
+      my_mf += (unsigned long long)deg;
+    }
+    emit_routed(found, u, deg, qout, qcount, qlout, lcount);
+  };
+  grid_expand_long(row_ptr, qlin, ln, s_long, op);
+  warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
   my_mf = warp_sum(my_mf);
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }
@@ -111,6 +117,8 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
   const int L = ctl->level;
   const int pout = L & 1;
   int32_t* qout = q + (size_t)pout * n;
+  int32_t* qlout = q + (size_t)(2 + pout) * n;
+  int32_t* lcount = &ctl->lsize[pout];
   const uint32_t* fin = rot(fbm, L - 1, nwords);
   uint32_t* fout = rot(fbm, L, nwords);
   uint32_t* fclr = rot(fbm, L + 1, nwords);
@@ -144,12 +152,13 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
         vbm[w] = vis | fm;
         fout[w] = fm;
       }
-      const int pos = warp_append(found, qcount);
+      int deg = 0;
       if (found) {
-        qout[pos] = u;
+        deg = row_ptr[u + 1] - row_ptr[u];
         dist[u] = L;
-        my_mf += (unsigned long long)(row_ptr[u + 1] - row_ptr[u]);
+        my_mf += (unsigned long long)deg;
       }
+      emit_routed(found, u, deg, qout, qcount, qlout, lcount);
     }
   }
   my_mf = warp_sum(my_mf);
@@ -164,7 +173,7 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditio
     return;
   }
   const int L = ctl->level, pout = L & 1;
-  const int nf = ctl->qsize[pout];
+  const int nf = ctl->qsize[pout] + ctl->lsize[pout];
   const unsigned long long mf = ctl->mf[pout];
   ctl->reached += mf;
   ctl->mu -= (long long)mf;
@@ -175,6 +184,7 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditio
     return;
   }
   ctl->qsize[pout ^ 1] = 0;
+  ctl->lsize[pout ^ 1] = 0;
   ctl->mf[pout ^ 1] = 0;
   int mode = ctl->mode;
   if (ctl->policy == DAWN_VARIANT_DO) {
@@ -204,7 +214,7 @@ void probe_ss(const void* p, LevelProbe* out) {
   out->level = c->level;
   out->mode = c->mode;
   out->done = c->done;
-  out->frontier = c->qsize[pin];
+  out->frontier = c->qsize[pin] + c->lsize[pin];
   out->frontier_edges = (int64_t)c->mf[pin];
   out->unvisited_edges = c->mu;
 }
@@ -216,7 +226,7 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   const int32_t n = g->n;
   int32_t nwords = (n + 31) / 32;
   long long m = g->m;
-  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * (size_t)n));
+  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 4 * (size_t)n));
   DAWN_CHECK(ensure(g->ss_bitmaps, sizeof(uint32_t) * 4 * (size_t)nwords));
   DAWN_CHECK(ensure(g->ss_ctl, sizeof(SsCtl)));
   DAWN_CHECK(ensure(g->ss_sources, sizeof(int32_t) * (size_t)nsrc));

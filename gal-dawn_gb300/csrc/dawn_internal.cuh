@@ -54,7 +54,8 @@ enum : int32_t { kModePush = 0, kModePull = 1 };
 // per-level kernel reads its parameters from here, so the same launches
 // (and the same captured CUDA graph) serve every level and every source.
 struct SsCtl {
-  int32_t qsize[2];             // frontier queue sizes by level parity
+  int32_t qsize[2];             // frontier queue sizes by level parity (short rows)
+  int32_t lsize[2];             // long-row frontier queue sizes (>= kLongRow entries)
   unsigned long long mf[2];     // out-degree sum of each queue
   long long mu;                 // degree sum of still-unvisited vertices
   unsigned long long reached;   // TEPS numerator of this source
@@ -141,7 +142,7 @@ struct dawn_graph {
   int32_t* t_col = nullptr;
 
   // single-source workspace
-  dawn::DevBuf ss_queues;   // 2 x n int32
+  dawn::DevBuf ss_queues;   // 4 x n int32: short queues [2], long-row queues [2]
   dawn::DevBuf ss_bitmaps;  // visited + 3 frontier bitmaps (words)
   dawn::DevBuf ss_ctl;      // SsCtl
   dawn::DevBuf ss_sources;  // int32 source list of the current call
@@ -154,6 +155,9 @@ struct dawn_graph {
   dawn::DevBuf bs_queues;   // active + touched queues
   dawn::DevBuf bs_ctl;
   dawn::DevBuf bs_sources;
+  dawn::DevBuf ul_static;       // vertices with an in-edge (pull work list)
+  int32_t ul_static_size = 0;
+  int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges
 
   // closeness reduction
   dawn::DevBuf cc_out;

@@ -50,6 +50,8 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
     ctl->source = s;
     ctl->qsize[0] = 0;
     ctl->qsize[1] = 0;
+    ctl->lsize[0] = 0;
+    ctl->lsize[1] = 0;
     ctl->level = 1;
     ctl->n_push = 0;
     ctl->n_pull = 0;
@@ -63,13 +65,17 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
     const int32_t u = col[k];
     if (last[u] == (unsigned long long)(k + 1)) {
       dist[u] = is_float ? __float_as_int(__ldg(wf + k)) : __ldg(wi + k);
-      q[atomicAdd(&ctl->qsize[0], 1)] = u;  // winners are unique: no dedup bit needed
+      // winners are unique: no dedup bit needed
+      if (row_ptr[u + 1] - row_ptr[u] >= kLongRow)
+        q[2 * (size_t)n + atomicAdd(&ctl->lsize[0], 1)] = u;
+      else
+        q[atomicAdd(&ctl->qsize[0], 1)] = u;
     }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     dist[s] = 0;
-    ctl->done = ctl->qsize[0] == 0;
+    ctl->done = ctl->qsize[0] + ctl->lsize[0] == 0;
   }
 }
 
@@ -81,11 +87,16 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
+  __shared__ LongTile s_long;
   if (ctl->done) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
   const int32_t* qin = q + (size_t)pin * n;
+  const int32_t* qlin = q + (size_t)(2 + pin) * n;
   int32_t* qout = q + (size_t)pout * n;
+  int32_t* qlout = q + (size_t)(2 + pout) * n;
+  int32_t* lcount = &ctl->lsize[pout];
+  const int ln = ctl->lsize[pin];
   uint32_t* inq_in = inq + (size_t)pin * nwords;
   uint32_t* inq_out = inq + (size_t)pout * nwords;
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
@@ -97,12 +108,12 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
   // The input queue's dedup bits are free again once the level has started:
   // this level claims in inq_out only.
   const size_t gstride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)qn; i += gstride) {
-    const int32_t v = qin[i];
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)(qn + ln); i += gstride) {
+    const int32_t v = i < (size_t)qn ? qin[i] : qlin[i - qn];
     atomicAnd(inq_in + (v >> 5), ~(1u << (v & 31)));
   }
 
-  warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], [&](int32_t v, int k, bool valid) {
+  auto op = [&](int32_t v, int k, bool valid) {
     bool found = false;
     int32_t u = -1;
     if (valid) {
@@ -115,9 +126,11 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
         }
       }
     }
-    const int pos = warp_append(found, qcount);
-    if (found) qout[pos] = u;
-  });
+    const int deg = found ? row_ptr[u + 1] - row_ptr[u] : 0;
+    emit_routed(found, u, deg, qout, qcount, qlout, lcount);
+  };
+  grid_expand_long(row_ptr, qlin, ln, s_long, op);
+  warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
 }
 
 __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop, int in_graph) {
@@ -130,12 +143,13 @@ __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditi
   ctl->n_push++;
   // The reference stops after n levels at most (src/algorithm/cpu/sssp.cpp:34);
   // with non-negative weights the queue empties long before.
-  if (ctl->qsize[pout] == 0 || L >= n) {
+  if (ctl->qsize[pout] + ctl->lsize[pout] == 0 || L >= n) {
     ctl->done = 1;
     if (in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
   ctl->qsize[pout ^ 1] = 0;
+  ctl->lsize[pout ^ 1] = 0;
   ctl->level = L + 1;
 }
 
@@ -151,7 +165,7 @@ void probe_sssp(const void* p, LevelProbe* out) {
   out->level = c->level;
   out->mode = kModePush;
   out->done = c->done;
-  out->frontier = c->qsize[(c->level - 1) & 1];
+  out->frontier = c->qsize[(c->level - 1) & 1] + c->lsize[(c->level - 1) & 1];
   out->frontier_edges = 0;
   out->unvisited_edges = 0;
 }
@@ -161,7 +175,7 @@ void probe_sssp(const void* p, LevelProbe* out) {
 dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist) {
   const int32_t n = g->n;
   const int32_t nwords = (n + 31) / 32;
-  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * (size_t)n));
+  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 4 * (size_t)n));
   DAWN_CHECK(ensure(g->ss_bitmaps, sizeof(uint32_t) * 4 * (size_t)nwords));
   DAWN_CHECK(ensure(g->ss_scratch, sizeof(unsigned long long) * (size_t)n));
   DAWN_CHECK(ensure(g->ss_ctl, sizeof(SsCtl)));

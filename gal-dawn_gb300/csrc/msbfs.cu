@@ -24,35 +24,54 @@ namespace dawn {
 namespace {
 
 struct BsCtl {
-  int32_t aq_size[2];          // active (frontier) queue sizes by level parity
+  int32_t aq_size[3];          // active (frontier) list sizes, rotating by level % 3
+  int32_t al_size[3];          // active long-row list sizes (>= kLongRow entries)
   int32_t tq_size;             // push: vertices touched this level
-  int32_t aq_prev;             // stale entries of the output frontier to clear
-  int32_t level, mode, done, policy;
-  unsigned long long mf[2];    // out-degree sums of the active queues
-  long long mu;                // degree sum of vertices not yet finished
-  long long mu_dec;            // degree of vertices finished this level
+  int32_t ul_size[2];          // unfinished-vertex lists (pull work lists)
+  int32_t ul_cur;              // list the next pull reads: -1 = the graph's static list
+  int32_t level, mode, done, policy, batch, nsrc, n_push, n_pull;
+  int32_t push_ratio;          // push while push_ratio * frontier edges < unfinished edges
+  int32_t pad;
+  unsigned long long mf[3];    // out-degree sums of the active lists
+  long long mu;                // in-degree sum of vertices not yet finished
+  long long mu_dec;            // in-degree of vertices finished this level
   unsigned long long reached;  // TEPS numerator of the batch
   unsigned long long full;     // this batch's source bits
-  int32_t batch, nsrc, n_push, n_pull;
   int32_t* dist_base;
   const int32_t* sources;
   unsigned long long total_reached;
-  int32_t total_levels, total_push, total_pull, pad;
+  int32_t total_levels, total_push, total_pull, pad2;
 };
 
-constexpr long long kPushRatio = 3;  // push while 3 * frontier edges < unfinished edges
+using u64 = unsigned long long;
 
-__device__ __forceinline__ void write_new_bits(int32_t* __restrict__ dist_base, int32_t n, int batch, int32_t u,
-                                               unsigned long long nw, int32_t level) {
+__device__ __forceinline__ u64 warp_or64(u64 x) {
+  const unsigned lo = __reduce_or_sync(kFull, (unsigned)x);
+  const unsigned hi = __reduce_or_sync(kFull, (unsigned)(x >> 32));
+  return ((u64)hi << 32) | lo;
+}
+
+// Warp-synchronous form: every lane walks the warp's union of new bits in
+// the same order, so each step stores one distance row's entries for the
+// warp's 32 vertices together.  All lanes must call it.
+__device__ __forceinline__ void write_new_bits_warp(int32_t* __restrict__ dist_base, int32_t n, int batch,
+                                                    int32_t u, u64 nw, int32_t level) {
+  u64 wm = warp_or64(nw);
   const size_t base = (size_t)batch * 64;
-  while (nw) {
-    const int b = __ffsll((long long)nw) - 1;
-    nw &= nw - 1;
-    dist_base[(base + b) * (size_t)n + u] = level;
+  while (wm) {
+    const int b = __ffsll((long long)wm) - 1;
+    wm &= wm - 1;
+    if ((nw >> b) & 1ull) dist_base[(base + b) * (size_t)n + u] = level;
   }
 }
 
-__global__ void __launch_bounds__(kBlock) bs_clear(unsigned long long* __restrict__ words, size_t count) {
+// Zero the frontier words listed in a stale active list (grid-stride).
+__device__ __forceinline__ void clear_listed(u64* __restrict__ fr, const int32_t* __restrict__ list, int cnt) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)cnt; i += stride) fr[list[i]] = 0ull;
+}
+
+__global__ void __launch_bounds__(kBlock) bs_clear(u64* __restrict__ words, size_t count) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   ulonglong2* w2 = reinterpret_cast<ulonglong2*>(words);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count / 2; i += stride)
@@ -61,9 +80,9 @@ __global__ void __launch_bounds__(kBlock) bs_clear(unsigned long long* __restric
 }
 
 __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
-                        unsigned long long* __restrict__ visit, unsigned long long* __restrict__ fr0,
+                        const int32_t* __restrict__ t_row_ptr, u64* __restrict__ visit, u64* __restrict__ fr0,
                         int32_t* __restrict__ aq0, int32_t n, long long m) {
-  __shared__ unsigned long long s_mf, s_reached, s_dec;
+  __shared__ u64 s_mf, s_reached, s_dec;
   const int b = threadIdx.x;
   const int batch = ctl->batch;
   const int nb = min(64, ctl->nsrc - batch * 64);
@@ -71,10 +90,11 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     s_mf = 0;
     s_reached = 0;
     s_dec = 0;
-    ctl->aq_size[0] = 0;
-    ctl->aq_size[1] = 0;
+    for (int i = 0; i < 3; i++) ctl->aq_size[i] = ctl->al_size[i] = 0;
     ctl->tq_size = 0;
-    ctl->aq_prev = 0;
+    ctl->ul_size[0] = 0;
+    ctl->ul_size[1] = 0;
+    ctl->ul_cur = -1;
     ctl->full = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
   }
   __syncthreads();
@@ -82,23 +102,26 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
   bool first = false;
   if (b < nb) {
     s = ctl->sources[batch * 64 + b];
-    const unsigned long long bit = 1ull << b;
+    const u64 bit = 1ull << b;
     atomicOr(visit + s, bit);
     first = atomicOr(fr0 + s, bit) == 0ull;
     ctl->dist_base[((size_t)batch * 64 + b) * (size_t)n + s] = 0;
-    atomicAdd(&s_reached, (unsigned long long)(row_ptr[s + 1] - row_ptr[s]));
+    atomicAdd(&s_reached, (u64)(row_ptr[s + 1] - row_ptr[s]));
   }
   __syncthreads();
   if (first) {
-    const unsigned long long deg = (unsigned long long)(row_ptr[s + 1] - row_ptr[s]);
-    aq0[atomicAdd(&ctl->aq_size[0], 1)] = s;
-    atomicAdd(&s_mf, deg);
-    if (visit[s] == ctl->full) atomicAdd(&s_dec, deg);
+    const int deg = row_ptr[s + 1] - row_ptr[s];
+    if (deg >= kLongRow)
+      aq0[3 * (size_t)n + atomicAdd(&ctl->al_size[0], 1)] = s;
+    else
+      aq0[atomicAdd(&ctl->aq_size[0], 1)] = s;
+    atomicAdd(&s_mf, (u64)deg);
+    if (visit[s] == ctl->full) atomicAdd(&s_dec, (u64)(t_row_ptr[s + 1] - t_row_ptr[s]));
   }
   __syncthreads();
   if (b == 0) {
+    for (int i = 0; i < 3; i++) ctl->mf[i] = 0;
     ctl->mf[0] = s_mf;
-    ctl->mf[1] = 0;
     ctl->reached = s_reached;
     ctl->mu = m - (long long)s_dec;
     ctl->mu_dec = 0;
@@ -112,119 +135,181 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
 
 // Per-thread accumulators of a level, flushed once per warp.
 struct LevelAcc {
-  unsigned long long mf = 0, reached = 0;
-  long long dec = 0;
-  __device__ __forceinline__ void flush(BsCtl* ctl, int pout) {
+  u64 mf = 0, reached = 0, dec = 0;
+  __device__ __forceinline__ void add(u64 out_deg, u64 in_deg, u64 nw, bool finished) {
+    mf += out_deg;
+    reached += out_deg * (u64)__popcll(nw);
+    if (finished) dec += in_deg;
+  }
+  __device__ __forceinline__ void flush(BsCtl* ctl, int slot) {
     mf = warp_sum(mf);
     reached = warp_sum(reached);
-    dec = (long long)warp_sum((unsigned long long)dec);
+    dec = warp_sum(dec);
     if (lane_id() == 0) {
-      if (mf) atomicAdd(&ctl->mf[pout], mf);
+      if (mf) atomicAdd(&ctl->mf[slot], mf);
       if (reached) atomicAdd(&ctl->reached, reached);
-      if (dec) atomicAdd(reinterpret_cast<unsigned long long*>(&ctl->mu_dec), (unsigned long long)dec);
+      if (dec) atomicAdd(reinterpret_cast<u64*>(&ctl->mu_dec), dec);
     }
   }
 };
 
+// Pull: every vertex of the unfinished list ORs the frontier words of its
+// in-neighbours.  Rows of >= 32 entries are swept by the whole warp (coalesced
+// col loads, early exit once no missing bit is left); shorter rows are
+// concatenated across the warp and OR-ed into per-lane shared-memory slots.
+// The vertex then owns its words: no global atomics.  The list is filtered
+// into the next unfinished list as it goes.
 __global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ row_ptr,
                                                   const int32_t* __restrict__ t_row_ptr,
                                                   const int32_t* __restrict__ t_col, BsCtl* __restrict__ ctl,
-                                                  unsigned long long* __restrict__ visit,
-                                                  unsigned long long* __restrict__ fr,
-                                                  int32_t* __restrict__ aq, int32_t n) {
+                                                  u64* __restrict__ visit, u64* __restrict__ fr,
+                                                  int32_t* __restrict__ aq, const int32_t* __restrict__ ul_static,
+                                                  int32_t ul_static_size, int32_t* __restrict__ ul, int32_t n) {
+  __shared__ int s_excl[kBlock / 32][32];
+  __shared__ int s_rs[kBlock / 32][32];
+  __shared__ u64 s_acc[kBlock / 32][32];
   if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
-  const int pin = (L - 1) & 1, pout = L & 1;
-  const unsigned long long* __restrict__ fin = fr + (size_t)pin * n;
-  unsigned long long* __restrict__ fout = fr + (size_t)pout * n;
-  int32_t* aq_out = aq + (size_t)pout * n;
-  const unsigned long long full = ctl->full;
+  const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n;
+  u64* __restrict__ fout = fr + (size_t)(L % 3) * n;
+  int32_t* aq_out = aq + (size_t)(L % 3) * n;
+  int32_t* al_out = aq + (size_t)(3 + L % 3) * n;
+  int32_t* aq_count = &ctl->aq_size[L % 3];
+  int32_t* al_count = &ctl->al_size[L % 3];
+  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3]);
+  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)(3 + (L + 1) % 3) * n, ctl->al_size[(L + 1) % 3]);
+  const int cur = ctl->ul_cur;
+  const int32_t* ul_in = cur < 0 ? ul_static : ul + (size_t)cur * n;
+  const int un = cur < 0 ? ul_static_size : ctl->ul_size[cur];
+  const int nxt = cur < 0 ? 0 : cur ^ 1;
+  int32_t* ul_out = ul + (size_t)nxt * n;
+  int32_t* ul_count = &ctl->ul_size[nxt];
+  const u64 full = ctl->full;
   const int batch = ctl->batch;
   int32_t* dist_base = ctl->dist_base;
+  const int lane = lane_id(), wib = threadIdx.x >> 5;
   LevelAcc acc;
-  // Grid-stride over all vertices; the trip count is uniform per warp so the
-  // warp-aggregated append below sees all 32 lanes.
-  const int total = gridDim.x * blockDim.x;
-  for (int base = blockIdx.x * blockDim.x; base < n; base += total) {
-    const int32_t u = base + threadIdx.x;
-    unsigned long long nw = 0;
-    if (u < n) {
-      const unsigned long long vis = visit[u];
-      if (vis != full) {
-        unsigned long long got = 0;
-        const int e = t_row_ptr[u + 1];
-        for (int k = t_row_ptr[u]; k < e; k++) {
-          got |= __ldg(fin + __ldg(t_col + k));
-          if ((got | vis) == full) break;
-        }
-        nw = got & ~vis;
-        if (nw) {
-          visit[u] = vis | nw;
-          const unsigned long long deg = (unsigned long long)(row_ptr[u + 1] - row_ptr[u]);
-          acc.mf += deg;
-          acc.reached += deg * (unsigned long long)__popcll(nw);
-          if ((vis | nw) == full) acc.dec += (long long)deg;
-          write_new_bits(dist_base, n, batch, u, nw, L);
-        }
-      }
-      fout[u] = nw;
+  for (int base = global_warp() * 32; base < un; base += num_warps() * 32) {
+    const int idx = base + lane;
+    int32_t u = -1;
+    u64 vis = full;
+    if (idx < un) {
+      u = ul_in[idx];
+      vis = visit[u];
     }
-    const int pos = warp_append(nw != 0, &ctl->aq_size[pout]);
-    if (nw) aq_out[pos] = u;
+    const bool active = vis != full;
+    int rs = 0, re = 0;
+    if (active) {
+      rs = t_row_ptr[u];
+      re = t_row_ptr[u + 1];
+    }
+    const int deg = re - rs;
+    u64 got = 0;
+    uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
+    while (big) {
+      const int leader = __ffs(big) - 1;
+      big &= big - 1;
+      const int s = __shfl_sync(kFull, rs, leader), e = __shfl_sync(kFull, re, leader);
+      const u64 lvis = __shfl_sync(kFull, vis, leader);
+      u64 w = 0;
+      for (int k0 = s; k0 < e; k0 += 32) {
+        const int k = k0 + lane;
+        if (k < e) w |= __ldg(fin + __ldg(t_col + k));
+        if ((warp_or64(w) | lvis) == full) break;
+      }
+      w = warp_or64(w);
+      if (lane == leader) got = w;
+    }
+    const int sdeg = deg < kWarpRow ? deg : 0;
+    const int incl = warp_incl_scan(sdeg);
+    const int total = __shfl_sync(kFull, incl, 31);
+    s_excl[wib][lane] = incl - sdeg;
+    s_rs[wib][lane] = rs;
+    s_acc[wib][lane] = 0ull;
+    __syncwarp();
+    for (int e0 = 0; e0 < total; e0 += 32) {
+      const int e = e0 + lane;
+      if (e < total) {
+        int lo = 0, hi = 31;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_excl[wib][mid] <= e) lo = mid; else hi = mid - 1;
+        }
+        const u64 x = __ldg(fin + __ldg(t_col + s_rs[wib][lo] + (e - s_excl[wib][lo])));
+        if (x) atomicOr(&s_acc[wib][lo], x);
+      }
+    }
+    __syncwarp();
+    if (sdeg > 0) got = s_acc[wib][lane];
+    __syncwarp();
+    const u64 nw = active ? (got & ~vis) : 0ull;
+    const bool still = active && ((vis | nw) != full);
+    int odeg = 0;
+    if (nw) {
+      visit[u] = vis | nw;
+      fout[u] = nw;
+      odeg = row_ptr[u + 1] - row_ptr[u];
+      acc.add((u64)odeg, (u64)deg, nw, !still);
+    }
+    write_new_bits_warp(dist_base, n, batch, u, nw, L);
+    const int pos = warp_append(still, ul_count);
+    if (still) ul_out[pos] = u;
+    emit_routed(nw != 0ull, u, odeg, aq_out, aq_count, al_out, al_count);
   }
-  acc.flush(ctl, pout);
+  acc.flush(ctl, L % 3);
 }
 
+// Push, phase 1: the active vertices' rows are dealt to warps; bits new to a
+// target are atomicOr-ed into `next` (skipped when `next` already holds
+// them), and the first toucher queues the target.
 __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restrict__ row_ptr,
                                                           const int32_t* __restrict__ col, BsCtl* __restrict__ ctl,
-                                                          const unsigned long long* __restrict__ visit,
-                                                          unsigned long long* __restrict__ fr,
-                                                          unsigned long long* __restrict__ nxt,
-                                                          int32_t* __restrict__ aq, int32_t* __restrict__ tq,
-                                                          int32_t n) {
+                                                          const u64* __restrict__ visit, u64* __restrict__ fr,
+                                                          u64* __restrict__ nxt, int32_t* __restrict__ aq,
+                                                          int32_t* __restrict__ tq, int32_t n) {
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
+  __shared__ LongTile s_long;
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
-  const int pin = (L - 1) & 1, pout = L & 1;
-  const unsigned long long* __restrict__ fin = fr + (size_t)pin * n;
-  unsigned long long* __restrict__ fout = fr + (size_t)pout * n;
-  const int32_t* aq_in = aq + (size_t)pin * n;
-  const int32_t* aq_old = aq + (size_t)pout * n;
-  const int qn = ctl->aq_size[pin];
-  // The output frontier still holds the words of two levels ago.
-  const int stale = ctl->aq_prev;
-  const size_t gstride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)stale; i += gstride)
-    fout[aq_old[i]] = 0ull;
+  const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n;
+  const int32_t* aq_in = aq + (size_t)((L - 1) % 3) * n;
+  const int32_t* al_in = aq + (size_t)(3 + (L - 1) % 3) * n;
+  const int qn = ctl->aq_size[(L - 1) % 3];
+  const int ln = ctl->al_size[(L - 1) % 3];
+  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3]);
+  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)(3 + (L + 1) % 3) * n, ctl->al_size[(L + 1) % 3]);
   const int wib = threadIdx.x >> 5;
-  warp_expand(row_ptr, aq_in, qn, s_excl[wib], s_rs[wib], s_v[wib], [&](int32_t v, int k, bool valid) {
+  auto op = [&](int32_t v, int k, bool valid) {
     bool first = false;
     int32_t u = -1;
     if (valid) {
       u = __ldg(col + k);
-      const unsigned long long bits = __ldg(fin + v) & ~__ldcg(visit + u);
+      u64 bits = __ldg(fin + v) & ~__ldcg(visit + u);
+      if (bits) bits &= ~__ldcg(nxt + u);
       if (bits) first = atomicOr(nxt + u, bits) == 0ull;
     }
     const int pos = warp_append(first, &ctl->tq_size);
     if (first) tq[pos] = u;
-  });
+  };
+  grid_expand_long(row_ptr, al_in, ln, s_long, op);
+  warp_expand(row_ptr, aq_in, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
 }
 
+// Push, phase 2: fold `next` into visited / frontier for the touched vertices.
 __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restrict__ row_ptr,
-                                                         BsCtl* __restrict__ ctl,
-                                                         unsigned long long* __restrict__ visit,
-                                                         unsigned long long* __restrict__ fr,
-                                                         unsigned long long* __restrict__ nxt,
+                                                         const int32_t* __restrict__ t_row_ptr,
+                                                         BsCtl* __restrict__ ctl, u64* __restrict__ visit,
+                                                         u64* __restrict__ fr, u64* __restrict__ nxt,
                                                          int32_t* __restrict__ aq, const int32_t* __restrict__ tq,
                                                          int32_t n) {
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
-  const int pout = L & 1;
-  unsigned long long* __restrict__ fout = fr + (size_t)pout * n;
-  int32_t* aq_out = aq + (size_t)pout * n;
-  const unsigned long long full = ctl->full;
+  u64* __restrict__ fout = fr + (size_t)(L % 3) * n;
+  int32_t* aq_out = aq + (size_t)(L % 3) * n;
+  int32_t* al_out = aq + (size_t)(3 + L % 3) * n;
+  const u64 full = ctl->full;
   const int batch = ctl->batch;
   int32_t* dist_base = ctl->dist_base;
   const int tn = ctl->tq_size;
@@ -232,28 +317,26 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
   const int total = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < tn; base += total) {
     const int i = base + threadIdx.x;
-    unsigned long long nw = 0;
+    u64 nw = 0;
     int32_t u = -1;
+    int odeg = 0;
     if (i < tn) {
       u = tq[i];
-      const unsigned long long x = nxt[u];
+      const u64 x = nxt[u];
       nxt[u] = 0ull;
-      const unsigned long long vis = visit[u];
+      const u64 vis = visit[u];
       nw = x & ~vis;
-      fout[u] = nw;
       if (nw) {
         visit[u] = vis | nw;
-        const unsigned long long deg = (unsigned long long)(row_ptr[u + 1] - row_ptr[u]);
-        acc.mf += deg;
-        acc.reached += deg * (unsigned long long)__popcll(nw);
-        if ((vis | nw) == full) acc.dec += (long long)deg;
-        write_new_bits(dist_base, n, batch, u, nw, L);
+        fout[u] = nw;
+        odeg = row_ptr[u + 1] - row_ptr[u];
+        acc.add((u64)odeg, (u64)(t_row_ptr[u + 1] - t_row_ptr[u]), nw, (vis | nw) == full);
       }
     }
-    const int pos = warp_append(nw != 0, &ctl->aq_size[pout]);
-    if (nw) aq_out[pos] = u;
+    write_new_bits_warp(dist_base, n, batch, u, nw, L);
+    emit_routed(nw != 0ull, u, odeg, aq_out, &ctl->aq_size[L % 3], al_out, &ctl->al_size[L % 3]);
   }
-  acc.flush(ctl, pout);
+  acc.flush(ctl, L % 3);
 }
 
 __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop, int in_graph) {
@@ -262,27 +345,32 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphCondition
     if (in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
-  const int L = ctl->level, pin = (L - 1) & 1, pout = L & 1;
-  if (ctl->mode == kModePush) ctl->n_push++; else ctl->n_pull++;
+  const int L = ctl->level;
+  if (ctl->mode == kModePush) {
+    ctl->n_push++;
+  } else {
+    ctl->n_pull++;
+    ctl->ul_cur = ctl->ul_cur < 0 ? 0 : ctl->ul_cur ^ 1;
+    ctl->ul_size[ctl->ul_cur ^ 1] = 0;
+  }
   ctl->mu -= ctl->mu_dec;
   ctl->mu_dec = 0;
-  const int nf = ctl->aq_size[pout];
+  ctl->tq_size = 0;
+  const int nf = ctl->aq_size[L % 3] + ctl->al_size[L % 3];
   if (nf == 0 || L >= n) {
     ctl->done = 1;
     if (in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
-  // Next level writes the frontier buffer this level read.
-  ctl->aq_prev = ctl->aq_size[pin];
-  ctl->aq_size[pin] = 0;
-  ctl->mf[pin] = 0;
-  ctl->tq_size = 0;
+  // Level L+1 writes list (L+1)%3, whose stale frontier words level L cleared.
+  ctl->aq_size[(L + 1) % 3] = 0;
+  ctl->al_size[(L + 1) % 3] = 0;
+  ctl->mf[(L + 1) % 3] = 0;
   int mode;
-  if (ctl->policy == DAWN_VARIANT_PUSH) {
+  if (ctl->policy == DAWN_VARIANT_PUSH)
     mode = kModePush;
-  } else {
-    mode = (long long)ctl->mf[pout] * kPushRatio < ctl->mu ? kModePush : kModePull;
-  }
+  else
+    mode = (long long)ctl->mf[L % 3] * ctl->push_ratio < ctl->mu ? kModePush : kModePull;
   ctl->mode = mode;
   ctl->level = L + 1;
 }
@@ -298,13 +386,49 @@ __global__ void bs_next(BsCtl* __restrict__ ctl) {
 
 void probe_bs(const void* p, LevelProbe* out) {
   const BsCtl* c = static_cast<const BsCtl*>(p);
-  const int pin = (c->level - 1) & 1;
+  const int pin = (c->level - 1) % 3;
   out->level = c->level;
   out->mode = c->mode;
   out->done = c->done;
-  out->frontier = c->aq_size[pin];
+  out->frontier = c->aq_size[pin] + c->al_size[pin];
   out->frontier_edges = (int64_t)c->mf[pin];
   out->unvisited_edges = c->mu;
+}
+
+// Static pull list: every vertex with an in-edge, in id order.
+__global__ void flag_in_degree(const int32_t* __restrict__ t_row_ptr, int32_t n, int64_t* __restrict__ flags) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride)
+    flags[i] = t_row_ptr[i + 1] > t_row_ptr[i] ? 1 : 0;
+}
+
+__global__ void scatter_flagged(const int64_t* __restrict__ flags, const int64_t* __restrict__ pos, int32_t n,
+                                int32_t* __restrict__ out) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride)
+    if (flags[i]) out[pos[i]] = (int32_t)i;
+}
+
+dawn_status build_static_list(dawn_graph* g) {
+  if (g->ul_static.p) return DAWN_OK;
+  const int32_t n = g->n;
+  int64_t* tmp = nullptr;
+  DAWN_CUDA(cudaMallocAsync(&tmp, sizeof(int64_t) * 2 * ((size_t)n + 1), g->stream));
+  int64_t* flags = tmp;
+  int64_t* pos = tmp + n + 1;
+  flag_in_degree<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->t_row_ptr, n, flags);
+  DAWN_CUDA(cudaGetLastError());
+  DAWN_CUDA(cudaMemsetAsync(flags + n, 0, sizeof(int64_t), g->stream));
+  DAWN_CHECK(exclusive_scan_i64(flags, pos, (int64_t)n + 1, g->stream));
+  DAWN_CHECK(ensure(g->ul_static, sizeof(int32_t) * (size_t)n));
+  scatter_flagged<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(flags, pos, n, g->ul_static.as<int32_t>());
+  DAWN_CUDA(cudaGetLastError());
+  int64_t cnt = 0;
+  DAWN_CUDA(cudaMemcpyAsync(&cnt, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, g->stream));
+  DAWN_CUDA(cudaFreeAsync(tmp, g->stream));
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  g->ul_static_size = (int32_t)cnt;
+  return DAWN_OK;
 }
 
 }  // namespace
@@ -312,9 +436,10 @@ void probe_bs(const void* p, LevelProbe* out) {
 dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist) {
   const int32_t n = g->n;
   const size_t nn = (size_t)n;
-  // words: visit | fr0 | fr1 | nxt
-  DAWN_CHECK(ensure(g->bs_words, sizeof(unsigned long long) * 4 * nn));
-  DAWN_CHECK(ensure(g->bs_queues, sizeof(int32_t) * 3 * nn));
+  DAWN_CHECK(build_static_list(g));
+  // words: visit | fr[3] | nxt ; lists: aq[3] | al[3] | tq | ul[2]
+  DAWN_CHECK(ensure(g->bs_words, sizeof(u64) * 5 * nn));
+  DAWN_CHECK(ensure(g->bs_queues, sizeof(int32_t) * 9 * nn));
   DAWN_CHECK(ensure(g->bs_ctl, sizeof(BsCtl)));
   DAWN_CHECK(ensure(g->bs_sources, sizeof(int32_t) * (size_t)nsrc));
   DAWN_CUDA(cudaMemcpyAsync(g->bs_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
@@ -323,15 +448,17 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   BsCtl c = {};
   c.nsrc = nsrc;
   c.policy = DAWN_VARIANT_BITSET;
+  c.push_ratio = g->bs_push_ratio;
   c.dist_base = d_dist;
   c.sources = g->bs_sources.as<int32_t>();
   DAWN_CUDA(cudaMemcpyAsync(g->bs_ctl.p, &c, sizeof(BsCtl), cudaMemcpyHostToDevice, g->stream));
 
   struct {
     BsCtl* ctl;
-    const int32_t *row_ptr, *col, *t_row_ptr, *t_col;
-    unsigned long long *words, *visit, *fr, *fr0, *nxt;
-    int32_t *aq, *aq0, *tq;
+    const int32_t *row_ptr, *col, *t_row_ptr, *t_col, *ul_static;
+    u64 *words, *visit, *fr, *fr0, *nxt;
+    int32_t *aq, *aq0, *tq, *ul;
+    int32_t ul_static_size;
     size_t nwords;
     int32_t n;
     long long m;
@@ -343,27 +470,30 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   a.col = g->col;
   a.t_row_ptr = g->t_row_ptr;
   a.t_col = g->t_col;
-  a.words = g->bs_words.as<unsigned long long>();
+  a.ul_static = g->ul_static.as<int32_t>();
+  a.ul_static_size = g->ul_static_size;
+  a.words = g->bs_words.as<u64>();
   a.visit = a.words;
   a.fr = a.words + nn;
   a.fr0 = a.fr;
-  a.nxt = a.words + 3 * nn;
+  a.nxt = a.words + 4 * nn;
   a.aq = g->bs_queues.as<int32_t>();
   a.aq0 = a.aq;
-  a.tq = a.aq + 2 * nn;
-  a.nwords = 4 * nn;
+  a.tq = a.aq + 6 * nn;
+  a.ul = a.aq + 7 * nn;
+  a.nwords = 5 * nn;
   a.n = n;
   a.m = g->m;
   a.handle = 0;
   a.in_graph = 0;
   void* clear_args[] = {&a.words, &a.nwords};
-  void* init_args[] = {&a.ctl, &a.row_ptr, &a.visit, &a.fr0, &a.aq0, &a.n, &a.m};
-  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.aq, &a.n};
+  void* init_args[] = {&a.ctl, &a.row_ptr, &a.t_row_ptr, &a.visit, &a.fr0, &a.aq0, &a.n, &a.m};
+  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.aq,
+                       &a.ul_static, &a.ul_static_size, &a.ul, &a.n};
   void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.tq, &a.n};
-  void* update_args[] = {&a.row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.tq, &a.n};
+  void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.tq, &a.n};
   void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
-
   const int sms = g->geo.sms;
   SsFamily fam;
   fam.npre = 2;

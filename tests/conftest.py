@@ -45,6 +45,9 @@ class Golden:
     def m(self):
         return int(self.col.shape[0])
 
+    def degrees(self):
+        return np.diff(self.row_ptr.astype(np.int64))
+
 
 def golden_all():
     return [Golden(p) for p in sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))]

@@ -100,3 +100,29 @@ def test_repeated_calls_reuse_graph():
             for v in (abi.VARIANT_BITSET, abi.VARIANT_DO):
                 d, _ = dg.bfs(srcs, variant=v)
                 assert np.array_equal(d, want)
+
+
+def hub_graph(nhub=1500, deg=2100, nleaf=5000, seed=12):
+    """A root joined to nhub hubs of ~deg leaves each: the second level is
+    more long rows than one shared-memory tile holds."""
+    rng = np.random.default_rng(seed)
+    n = 1 + nhub + nleaf
+    src = [np.zeros(nhub, np.int64)]
+    dst = [1 + np.arange(nhub)]
+    for h in range(nhub):
+        leaves = 1 + nhub + rng.choice(nleaf, deg, replace=False)
+        src.append(np.full(deg, 1 + h))
+        dst.append(leaves)
+    src = np.concatenate(src)
+    dst = np.concatenate(dst)
+    s2 = np.concatenate([src, dst])
+    d2 = np.concatenate([dst, src])
+    order = np.lexsort((d2, s2))
+    rp = np.concatenate([[0], np.cumsum(np.bincount(s2, minlength=n))]).astype(np.int32)
+    return gen.CsrGraph(n, rp, d2[order].astype(np.int32), symmetric=True)
+
+
+def test_long_rows_span_tiles():
+    g = hub_graph()
+    check(g, np.array([0, 1, 1 + 1500 + 7], np.int32))
+    check(g, np.arange(0, 200, dtype=np.int32), variants=[abi.VARIANT_BITSET])

@@ -82,3 +82,12 @@ def test_unweighted_graph_rejected():
         with pytest.raises(abi.DawnError) as e:
             dg.sssp([0])
         assert e.value.status == abi.ERR_UNSUPPORTED
+
+
+def test_long_rows_weighted():
+    from test_gpu_bfs import hub_graph
+    g = hub_graph(nhub=1200, deg=2100, nleaf=4000, seed=13)
+    w = (np.arange(g.m) % 17 + 1).astype(np.int32)
+    # symmetric weights are not needed for SSSP parity
+    g.w_i32, g.w_f32 = w, w.astype(np.float32)
+    check(g, np.array([0, 5, 1300], np.int32))
