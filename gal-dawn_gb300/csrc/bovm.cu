@@ -37,7 +37,8 @@ __global__ void __launch_bounds__(kBlock) bfs_clear(SsCtl* __restrict__ ctl, uin
 }
 
 __global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
-                         int32_t* __restrict__ q, uint32_t* __restrict__ vbm, int32_t n, long long m) {
+                         int32_t* __restrict__ q, Seg* __restrict__ segs, uint32_t* __restrict__ vbm, int32_t n,
+                         long long m) {
   if (threadIdx.x != 0) return;
   const int32_t s = ctl->sources[ctl->src_idx];
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
@@ -45,12 +46,18 @@ __global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ ro
   ctl->source = s;
   dist[s] = 0;
   vbm[s >> 5] |= 1u << (s & 31);
-  const bool is_long = deg >= kLongRow;
-  q[(is_long ? 2 : 0) * (size_t)n] = s;
-  ctl->qsize[0] = is_long ? 0 : 1;
-  ctl->lsize[0] = is_long ? 1 : 0;
+  if (deg >= kLongRow) {
+    const int nseg = (deg + kSeg - 1) / kSeg;
+    for (int j = 0; j < nseg; j++) segs[j] = Seg{s, row_ptr[s] + j * kSeg};
+    ctl->qsize[0] = 0;
+    ctl->lpack[0] = (1ull << 32) | (unsigned)nseg;
+  } else {
+    q[0] = s;
+    ctl->qsize[0] = 1;
+    ctl->lpack[0] = 0;
+  }
   ctl->qsize[1] = 0;
-  ctl->lsize[1] = 0;
+  ctl->lpack[1] = 0;
   ctl->mf[0] = (unsigned long long)deg;
   ctl->mf[1] = 0;
   ctl->mu = m - deg;
@@ -65,25 +72,25 @@ __global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ ro
 
 __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ row_ptr,
                                                    const int32_t* __restrict__ col, SsCtl* __restrict__ ctl,
-                                                   int32_t* __restrict__ q, uint32_t* __restrict__ vbm,
-                                                   uint32_t* __restrict__ fbm, int32_t n, int32_t nwords) {
+                                                   int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
+                                                   uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
+                                                   int32_t n, int32_t nwords) {
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
-  __shared__ LongTile s_long;
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
   const int32_t* qin = q + (size_t)pin * n;
-  const int32_t* qlin = q + (size_t)(2 + pin) * n;
+  const Seg* sin = segs + (size_t)pin * segcap;
   int32_t* qout = q + (size_t)pout * n;
-  int32_t* qlout = q + (size_t)(2 + pout) * n;
+  Seg* sout = segs + (size_t)pout * segcap;
   uint32_t* fout = rot(fbm, L, nwords);
   uint32_t* fclr = rot(fbm, L + 1, nwords);
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
   int32_t* qcount = &ctl->qsize[pout];
-  int32_t* lcount = &ctl->lsize[pout];
-  const int qn = ctl->qsize[pin], ln = ctl->lsize[pin];
+  unsigned long long* lpack = &ctl->lpack[pout];
+  const int qn = ctl->qsize[pin], ln = seg_count(ctl->lpack[pin]);
   const int lane = lane_id(), wib = threadIdx.x >> 5;
 
   const size_t gstride = (size_t)gridDim.x * blockDim.x;
@@ -93,16 +100,17 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   auto op = [&](int32_t, int k, bool valid) {
     const int32_t u = valid ? __ldg(col + k) : -1;
     const bool found = valid && claim_bit(vbm, u);
-    int deg = 0;
+    int deg = 0, rs = 0;
     if (found) {
-      deg = row_ptr[u + 1] - row_ptr[u];
+      rs = row_ptr[u];
+      deg = row_ptr[u + 1] - rs;
       dist[u] = L;
       atomicOr(fout + (u >> 5), 1u << (u & 31));
       my_mf += (unsigned long long)deg;
     }
-    emit_routed(found, u, deg, qout, qcount, qlout, lcount);
+    emit_routed(found, u, deg, rs, qout, qcount, sout, lpack);
   };
-  grid_expand_long(row_ptr, qlin, ln, s_long, op);
+  seg_expand(row_ptr, sin, ln, op);
   warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
   my_mf = warp_sum(my_mf);
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
@@ -111,14 +119,15 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
 __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ row_ptr,
                                                    const int32_t* __restrict__ t_row_ptr,
                                                    const int32_t* __restrict__ t_col, SsCtl* __restrict__ ctl,
-                                                   int32_t* __restrict__ q, uint32_t* __restrict__ vbm,
-                                                   uint32_t* __restrict__ fbm, int32_t n, int32_t nwords) {
+                                                   int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
+                                                   uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
+                                                   int32_t n, int32_t nwords) {
   if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
   const int pout = L & 1;
   int32_t* qout = q + (size_t)pout * n;
-  int32_t* qlout = q + (size_t)(2 + pout) * n;
-  int32_t* lcount = &ctl->lsize[pout];
+  Seg* sout = segs + (size_t)pout * segcap;
+  unsigned long long* lpack = &ctl->lpack[pout];
   const uint32_t* fin = rot(fbm, L - 1, nwords);
   uint32_t* fout = rot(fbm, L, nwords);
   uint32_t* fclr = rot(fbm, L + 1, nwords);
@@ -152,13 +161,14 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
         vbm[w] = vis | fm;
         fout[w] = fm;
       }
-      int deg = 0;
+      int deg = 0, rs = 0;
       if (found) {
-        deg = row_ptr[u + 1] - row_ptr[u];
+        rs = row_ptr[u];
+        deg = row_ptr[u + 1] - rs;
         dist[u] = L;
         my_mf += (unsigned long long)deg;
       }
-      emit_routed(found, u, deg, qout, qcount, qlout, lcount);
+      emit_routed(found, u, deg, rs, qout, qcount, sout, lpack);
     }
   }
   my_mf = warp_sum(my_mf);
@@ -173,7 +183,7 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditio
     return;
   }
   const int L = ctl->level, pout = L & 1;
-  const int nf = ctl->qsize[pout] + ctl->lsize[pout];
+  const int nf = ctl->qsize[pout] + long_vertices(ctl->lpack[pout]);
   const unsigned long long mf = ctl->mf[pout];
   ctl->reached += mf;
   ctl->mu -= (long long)mf;
@@ -184,7 +194,7 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditio
     return;
   }
   ctl->qsize[pout ^ 1] = 0;
-  ctl->lsize[pout ^ 1] = 0;
+  ctl->lpack[pout ^ 1] = 0;
   ctl->mf[pout ^ 1] = 0;
   int mode = ctl->mode;
   if (ctl->policy == DAWN_VARIANT_DO) {
@@ -214,7 +224,7 @@ void probe_ss(const void* p, LevelProbe* out) {
   out->level = c->level;
   out->mode = c->mode;
   out->done = c->done;
-  out->frontier = c->qsize[pin] + c->lsize[pin];
+  out->frontier = c->qsize[pin] + (int64_t)(c->lpack[pin] >> 32);
   out->frontier_edges = (int64_t)c->mf[pin];
   out->unvisited_edges = c->mu;
 }
@@ -226,7 +236,9 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   const int32_t n = g->n;
   int32_t nwords = (n + 31) / 32;
   long long m = g->m;
-  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 4 * (size_t)n));
+  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * (size_t)n));
+  size_t segcap = seg_capacity(n, m);
+  DAWN_CHECK(ensure(g->ss_segs, sizeof(Seg) * 2 * segcap));
   DAWN_CHECK(ensure(g->ss_bitmaps, sizeof(uint32_t) * 4 * (size_t)nwords));
   DAWN_CHECK(ensure(g->ss_ctl, sizeof(SsCtl)));
   DAWN_CHECK(ensure(g->ss_sources, sizeof(int32_t) * (size_t)nsrc));
@@ -243,6 +255,8 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
     SsCtl* ctl;
     const int32_t *row_ptr, *col, *t_row_ptr, *t_col;
     int32_t* q;
+    Seg* segs;
+    size_t segcap;
     uint32_t *bitmaps, *vbm, *fbm;
     int32_t n, nwords;
     long long m;
@@ -255,6 +269,8 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   a.t_row_ptr = g->t_row_ptr;
   a.t_col = g->t_col;
   a.q = g->ss_queues.as<int32_t>();
+  a.segs = g->ss_segs.as<Seg>();
+  a.segcap = segcap;
   a.bitmaps = g->ss_bitmaps.as<uint32_t>();
   a.vbm = a.bitmaps;
   a.fbm = a.bitmaps + nwords;
@@ -264,9 +280,10 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   a.handle = 0;
   a.in_graph = 0;
   void* clear_args[] = {&a.ctl, &a.bitmaps, &a.n, &a.nwords};
-  void* init_args[] = {&a.ctl, &a.row_ptr, &a.q, &a.vbm, &a.n, &a.m};
-  void* push_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.vbm, &a.fbm, &a.n, &a.nwords};
-  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.q, &a.vbm, &a.fbm, &a.n, &a.nwords};
+  void* init_args[] = {&a.ctl, &a.row_ptr, &a.q, &a.segs, &a.vbm, &a.n, &a.m};
+  void* push_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm, &a.n, &a.nwords};
+  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm,
+                       &a.n, &a.nwords};
   void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
 

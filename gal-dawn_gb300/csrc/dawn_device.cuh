@@ -133,100 +133,62 @@ __device__ __forceinline__ void warp_expand(const int32_t* __restrict__ row_ptr,
 
 namespace dawn {
 
-constexpr int kLongRow = 2048;  // rows this long are dealt to the whole grid
-constexpr int kLongTile = 1024; // long rows staged per shared-memory tile
+// Rows of at least kLongRow entries leave the vertex queues: when such a
+// vertex is discovered it is entered as ceil(deg / kSeg) segments of at most
+// kSeg consecutive CSR positions, and the next expansion deals segments to
+// warps, so a hub's row is spread over many warps instead of one.
+constexpr int kSeg = 128;
+constexpr int kLongRow = kSeg;
 
-// Shared-memory staging of a tile of long rows for grid_expand_long.
-struct LongTile {
-  int v[kLongTile];
-  int rs[kLongTile];
-  long long off[kLongTile + 1];
+struct Seg {
+  int32_t v;   // vertex
+  int32_t k0;  // first CSR position of the segment
 };
 
-// Deals the edges of a list of long rows over every warp of the grid: each
-// CTA stages up to kLongTile rows (vertex, row start, exclusive edge offset)
-// in shared memory, then warp w takes edges [32 c, 32 c + 32) of the
-// concatenated rows for c = w, w + warps, ...  One lane per edge, coalesced
-// within a row.  op(v, k, valid) as in warp_expand.  Every thread of the CTA
-// must call this (it synchronises the CTA).
-template <class Op>
-__device__ __forceinline__ void grid_expand_long(const int32_t* __restrict__ row_ptr,
-                                                 const int32_t* __restrict__ list, int cnt, LongTile& t,
-                                                 Op&& op) {
-  const int lane = lane_id();
-  for (int tile = 0; tile < cnt; tile += kLongTile) {
-    const int tc = min(kLongTile, cnt - tile);
-    __syncthreads();
-    // Block-wide exclusive scan of the row lengths (blockDim.x == kBlock).
-    constexpr int kPer = kLongTile / kBlock;
-    long long local[kPer];
-    long long sum = 0;
-#pragma unroll
-    for (int j = 0; j < kPer; j++) {
-      const int i = threadIdx.x * kPer + j;
-      long long d = 0;
-      if (i < tc) {
-        const int32_t v = list[tile + i];
-        const int rs = row_ptr[v];
-        t.v[i] = v;
-        t.rs[i] = rs;
-        d = row_ptr[v + 1] - rs;
-      }
-      local[j] = sum;
-      sum += d;
-    }
-    __shared__ long long s_warp[kBlock / 32];
-    long long incl = sum;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const long long y = __shfl_up_sync(kFull, incl, d);
-      if (lane >= d) incl += y;
-    }
-    if (lane == 31) s_warp[threadIdx.x >> 5] = incl;
-    __syncthreads();
-    long long before = incl - sum;
-    for (int w = 0; w < (int)(threadIdx.x >> 5); w++) before += s_warp[w];
-#pragma unroll
-    for (int j = 0; j < kPer; j++) {
-      const int i = threadIdx.x * kPer + j;
-      if (i < tc) t.off[i] = before + local[j];
-    }
-    if (threadIdx.x == blockDim.x - 1) t.off[tc] = before + sum;
-    __syncthreads();
-    const long long total = t.off[tc];
-    for (long long e0 = (long long)global_warp() * 32; e0 < total; e0 += (long long)num_warps() * 32) {
-      const long long e = e0 + lane;
-      int32_t v = -1;
-      int k = 0;
-      if (e < total) {
-        int lo = 0, hi = tc - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (t.off[mid] <= e) lo = mid; else hi = mid - 1;
-        }
-        v = t.v[lo];
-        k = t.rs[lo] + (int)(e - t.off[lo]);
-      }
-      op(v, k, e < total);
-    }
+// Capacity of one level's segment list.  A vertex enters a level's list at
+// most once and a row of d >= kLongRow entries adds ceil(d / kSeg) <=
+// d / kSeg + 1 <= 2 d / kSeg segments, so 2 m / kSeg bounds the list.
+__host__ __device__ inline size_t seg_capacity(int32_t n, long long m) {
+  (void)n;
+  return 2 * (size_t)(m / kSeg) + 64;
+}
+
+// Queues a discovered vertex: short rows as a vertex, long rows as segments.
+// lpack packs (long vertices << 32 | segments) so one atomicAdd per warp
+// reserves the warp's segment slots.  All 32 lanes must call it.
+__device__ __forceinline__ void emit_routed(bool found, int32_t u, int deg, int rs, int32_t* __restrict__ q_short,
+                                            int32_t* short_count, Seg* __restrict__ segs,
+                                            unsigned long long* lpack) {
+  const bool is_long = found && deg >= kLongRow;
+  const bool is_short = found && !is_long;
+  const int p = warp_append(is_short, short_count);
+  if (is_short) q_short[p] = u;
+  const uint32_t lm = __ballot_sync(kFull, is_long);
+  if (lm) {
+    const int nseg = is_long ? (deg + kSeg - 1) / kSeg : 0;
+    const int incl = warp_incl_scan(nseg);
+    const int tot = __shfl_sync(kFull, incl, 31);
+    unsigned long long base = 0;
+    if (lane_id() == 0) base = atomicAdd(lpack, ((unsigned long long)__popc(lm) << 32) | (unsigned)tot);
+    const uint32_t b = (uint32_t)__shfl_sync(kFull, base, 0);
+    for (int j = 0; j < nseg; j++) segs[b + incl - nseg + j] = Seg{u, rs + j * kSeg};
   }
 }
 
-}  // namespace dawn
+__device__ __forceinline__ int seg_count(unsigned long long lpack) { return (int)(uint32_t)lpack; }
+__device__ __forceinline__ int long_vertices(unsigned long long lpack) { return (int)(lpack >> 32); }
 
-namespace dawn {
-
-// Appends a discovered vertex to the short-row or the long-row list by its
-// out-degree.  All 32 lanes must call it.
-__device__ __forceinline__ void emit_routed(bool found, int32_t u, int deg, int32_t* __restrict__ q_short,
-                                            int32_t* short_count, int32_t* __restrict__ q_long,
-                                            int32_t* long_count) {
-  const bool is_long = found && deg >= kLongRow;
-  const bool is_short = found && !is_long;
-  int p = warp_append(is_short, short_count);
-  if (is_short) q_short[p] = u;
-  p = warp_append(is_long, long_count);
-  if (is_long) q_long[p] = u;
+// Deals segments to warps (one segment per warp at a time, one lane per
+// edge).  op(v, k, valid) as in warp_expand.
+template <class Op>
+__device__ __forceinline__ void seg_expand(const int32_t* __restrict__ row_ptr, const Seg* __restrict__ segs,
+                                           int nsegs, Op&& op) {
+  const int lane = lane_id();
+  for (int i = global_warp(); i < nsegs; i += num_warps()) {
+    const Seg sg = segs[i];
+    const int e = min(sg.k0 + kSeg, row_ptr[sg.v + 1]);
+    for (int k0 = sg.k0; k0 < e; k0 += 32) op(sg.v, k0 + lane, k0 + lane < e);
+  }
 }
 
 }  // namespace dawn

@@ -55,7 +55,7 @@ enum : int32_t { kModePush = 0, kModePull = 1 };
 // (and the same captured CUDA graph) serve every level and every source.
 struct SsCtl {
   int32_t qsize[2];             // frontier queue sizes by level parity (short rows)
-  int32_t lsize[2];             // long-row frontier queue sizes (>= kLongRow entries)
+  unsigned long long lpack[2];  // long rows: (vertices << 32) | segments, by parity
   unsigned long long mf[2];     // out-degree sum of each queue
   long long mu;                 // degree sum of still-unvisited vertices
   unsigned long long reached;   // TEPS numerator of this source
@@ -142,7 +142,8 @@ struct dawn_graph {
   int32_t* t_col = nullptr;
 
   // single-source workspace
-  dawn::DevBuf ss_queues;   // 4 x n int32: short queues [2], long-row queues [2]
+  dawn::DevBuf ss_queues;   // 2 x n int32 short-row queues
+  dawn::DevBuf ss_segs;     // 2 x seg_capacity long-row segments
   dawn::DevBuf ss_bitmaps;  // visited + 3 frontier bitmaps (words)
   dawn::DevBuf ss_ctl;      // SsCtl
   dawn::DevBuf ss_sources;  // int32 source list of the current call
@@ -155,6 +156,7 @@ struct dawn_graph {
   dawn::DevBuf bs_queues;   // active + touched queues
   dawn::DevBuf bs_ctl;
   dawn::DevBuf bs_sources;
+  dawn::DevBuf bs_segs;         // 3 x seg_capacity long-row segments
   dawn::DevBuf ul_static;       // vertices with an in-edge (pull work list)
   int32_t ul_static_size = 0;
   int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges

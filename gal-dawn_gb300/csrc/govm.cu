@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
                                                     const int32_t* __restrict__ col, const int32_t* __restrict__ wi,
                                                     const float* __restrict__ wf, int is_float,
                                                     unsigned long long* __restrict__ last, int32_t* __restrict__ q,
-                                                    int32_t n) {
+                                                    Seg* __restrict__ segs, int32_t n) {
   const int32_t s = ctl->sources[ctl->src_idx];
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
   const int rs = row_ptr[s], re = row_ptr[s + 1];
@@ -50,8 +50,8 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
     ctl->source = s;
     ctl->qsize[0] = 0;
     ctl->qsize[1] = 0;
-    ctl->lsize[0] = 0;
-    ctl->lsize[1] = 0;
+    ctl->lpack[0] = 0;
+    ctl->lpack[1] = 0;
     ctl->level = 1;
     ctl->n_push = 0;
     ctl->n_pull = 0;
@@ -66,16 +66,20 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
     if (last[u] == (unsigned long long)(k + 1)) {
       dist[u] = is_float ? __float_as_int(__ldg(wf + k)) : __ldg(wi + k);
       // winners are unique: no dedup bit needed
-      if (row_ptr[u + 1] - row_ptr[u] >= kLongRow)
-        q[2 * (size_t)n + atomicAdd(&ctl->lsize[0], 1)] = u;
-      else
+      const int urs = row_ptr[u], udeg = row_ptr[u + 1] - urs;
+      if (udeg >= kLongRow) {
+        const int nseg = (udeg + kSeg - 1) / kSeg;
+        const unsigned long long old = atomicAdd(&ctl->lpack[0], (1ull << 32) | (unsigned)nseg);
+        for (int j = 0; j < nseg; j++) segs[(uint32_t)old + j] = Seg{u, urs + j * kSeg};
+      } else {
         q[atomicAdd(&ctl->qsize[0], 1)] = u;
+      }
     }
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     dist[s] = 0;
-    ctl->done = ctl->qsize[0] + ctl->lsize[0] == 0;
+    ctl->done = ctl->qsize[0] == 0 && ctl->lpack[0] == 0;
   }
 }
 
@@ -83,20 +87,20 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
                                                      const int32_t* __restrict__ col, const int32_t* __restrict__ wi,
                                                      const float* __restrict__ wf, int is_float,
                                                      SsCtl* __restrict__ ctl, int32_t* __restrict__ q,
+                                                     Seg* __restrict__ segs, size_t segcap,
                                                      uint32_t* __restrict__ inq, int32_t n, int32_t nwords) {
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
-  __shared__ LongTile s_long;
   if (ctl->done) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
   const int32_t* qin = q + (size_t)pin * n;
-  const int32_t* qlin = q + (size_t)(2 + pin) * n;
+  const Seg* sin = segs + (size_t)pin * segcap;
   int32_t* qout = q + (size_t)pout * n;
-  int32_t* qlout = q + (size_t)(2 + pout) * n;
-  int32_t* lcount = &ctl->lsize[pout];
-  const int ln = ctl->lsize[pin];
+  Seg* sout = segs + (size_t)pout * segcap;
+  unsigned long long* lpack = &ctl->lpack[pout];
+  const int ln = seg_count(ctl->lpack[pin]);
   uint32_t* inq_in = inq + (size_t)pin * nwords;
   uint32_t* inq_out = inq + (size_t)pout * nwords;
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
@@ -109,7 +113,7 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
   // this level claims in inq_out only.
   const size_t gstride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)(qn + ln); i += gstride) {
-    const int32_t v = i < (size_t)qn ? qin[i] : qlin[i - qn];
+    const int32_t v = i < (size_t)qn ? qin[i] : sin[i - qn].v;
     atomicAnd(inq_in + (v >> 5), ~(1u << (v & 31)));
   }
 
@@ -126,10 +130,14 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
         }
       }
     }
-    const int deg = found ? row_ptr[u + 1] - row_ptr[u] : 0;
-    emit_routed(found, u, deg, qout, qcount, qlout, lcount);
+    int deg = 0, rs = 0;
+    if (found) {
+      rs = row_ptr[u];
+      deg = row_ptr[u + 1] - rs;
+    }
+    emit_routed(found, u, deg, rs, qout, qcount, sout, lpack);
   };
-  grid_expand_long(row_ptr, qlin, ln, s_long, op);
+  seg_expand(row_ptr, sin, ln, op);
   warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
 }
 
@@ -143,13 +151,13 @@ __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditi
   ctl->n_push++;
   // The reference stops after n levels at most (src/algorithm/cpu/sssp.cpp:34);
   // with non-negative weights the queue empties long before.
-  if (ctl->qsize[pout] + ctl->lsize[pout] == 0 || L >= n) {
+  if ((ctl->qsize[pout] == 0 && ctl->lpack[pout] == 0) || L >= n) {
     ctl->done = 1;
     if (in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
   ctl->qsize[pout ^ 1] = 0;
-  ctl->lsize[pout ^ 1] = 0;
+  ctl->lpack[pout ^ 1] = 0;
   ctl->level = L + 1;
 }
 
@@ -165,7 +173,7 @@ void probe_sssp(const void* p, LevelProbe* out) {
   out->level = c->level;
   out->mode = kModePush;
   out->done = c->done;
-  out->frontier = c->qsize[(c->level - 1) & 1] + c->lsize[(c->level - 1) & 1];
+  out->frontier = c->qsize[(c->level - 1) & 1] + (int64_t)(c->lpack[(c->level - 1) & 1] >> 32);
   out->frontier_edges = 0;
   out->unvisited_edges = 0;
 }
@@ -175,7 +183,9 @@ void probe_sssp(const void* p, LevelProbe* out) {
 dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist) {
   const int32_t n = g->n;
   const int32_t nwords = (n + 31) / 32;
-  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 4 * (size_t)n));
+  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * (size_t)n));
+  size_t segcap = seg_capacity(n, g->m);
+  DAWN_CHECK(ensure(g->ss_segs, sizeof(Seg) * 2 * segcap));
   DAWN_CHECK(ensure(g->ss_bitmaps, sizeof(uint32_t) * 4 * (size_t)nwords));
   DAWN_CHECK(ensure(g->ss_scratch, sizeof(unsigned long long) * (size_t)n));
   DAWN_CHECK(ensure(g->ss_ctl, sizeof(SsCtl)));
@@ -198,6 +208,8 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
     int is_float;
     unsigned long long* last;
     int32_t* q;
+    Seg* segs;
+    size_t segcap;
     uint32_t* inq;
     int32_t n, nwords, inf;
     cudaGraphConditionalHandle handle;
@@ -211,6 +223,8 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   a.is_float = is_float;
   a.last = g->ss_scratch.as<unsigned long long>();
   a.q = g->ss_queues.as<int32_t>();
+  a.segs = g->ss_segs.as<Seg>();
+  a.segcap = segcap;
   a.inq = g->ss_bitmaps.as<uint32_t>();
   a.n = n;
   a.nwords = nwords;
@@ -218,8 +232,9 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   a.handle = 0;
   a.in_graph = 0;
   void* clear_args[] = {&a.ctl, &a.inq, &a.n, &a.nwords, &a.inf};
-  void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.last, &a.q, &a.n};
-  void* relax_args[] = {&a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.ctl, &a.q, &a.inq, &a.n, &a.nwords};
+  void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.last, &a.q, &a.segs, &a.n};
+  void* relax_args[] = {&a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.ctl, &a.q, &a.segs, &a.segcap,
+                        &a.inq, &a.n, &a.nwords};
   void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
 

@@ -25,7 +25,8 @@ namespace {
 
 struct BsCtl {
   int32_t aq_size[3];          // active (frontier) list sizes, rotating by level % 3
-  int32_t al_size[3];          // active long-row list sizes (>= kLongRow entries)
+  int32_t pad0;
+  unsigned long long alpack[3]; // active long rows: (vertices << 32) | segments
   int32_t tq_size;             // push: vertices touched this level
   int32_t ul_size[2];          // unfinished-vertex lists (pull work lists)
   int32_t ul_cur;              // list the next pull reads: -1 = the graph's static list
@@ -65,10 +66,14 @@ __device__ __forceinline__ void write_new_bits_warp(int32_t* __restrict__ dist_b
   }
 }
 
-// Zero the frontier words listed in a stale active list (grid-stride).
-__device__ __forceinline__ void clear_listed(u64* __restrict__ fr, const int32_t* __restrict__ list, int cnt) {
+// Zero the frontier words listed in a stale active list and its segment
+// list (grid-stride).
+__device__ __forceinline__ void clear_listed(u64* __restrict__ fr, const int32_t* __restrict__ list, int cnt,
+                                             const Seg* __restrict__ segs, int nsegs) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)cnt; i += stride) fr[list[i]] = 0ull;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nsegs; i += stride)
+    fr[segs[i].v] = 0ull;
 }
 
 __global__ void __launch_bounds__(kBlock) bs_clear(u64* __restrict__ words, size_t count) {
@@ -81,7 +86,7 @@ __global__ void __launch_bounds__(kBlock) bs_clear(u64* __restrict__ words, size
 
 __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
                         const int32_t* __restrict__ t_row_ptr, u64* __restrict__ visit, u64* __restrict__ fr0,
-                        int32_t* __restrict__ aq0, int32_t n, long long m) {
+                        int32_t* __restrict__ aq0, Seg* __restrict__ segs0, int32_t n, long long m) {
   __shared__ u64 s_mf, s_reached, s_dec;
   const int b = threadIdx.x;
   const int batch = ctl->batch;
@@ -90,7 +95,10 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     s_mf = 0;
     s_reached = 0;
     s_dec = 0;
-    for (int i = 0; i < 3; i++) ctl->aq_size[i] = ctl->al_size[i] = 0;
+    for (int i = 0; i < 3; i++) {
+      ctl->aq_size[i] = 0;
+      ctl->alpack[i] = 0;
+    }
     ctl->tq_size = 0;
     ctl->ul_size[0] = 0;
     ctl->ul_size[1] = 0;
@@ -110,11 +118,14 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
   }
   __syncthreads();
   if (first) {
-    const int deg = row_ptr[s + 1] - row_ptr[s];
-    if (deg >= kLongRow)
-      aq0[3 * (size_t)n + atomicAdd(&ctl->al_size[0], 1)] = s;
-    else
+    const int rs = row_ptr[s], deg = row_ptr[s + 1] - rs;
+    if (deg >= kLongRow) {
+      const int nseg = (deg + kSeg - 1) / kSeg;
+      const u64 old = atomicAdd(&ctl->alpack[0], (1ull << 32) | (unsigned)nseg);
+      for (int j = 0; j < nseg; j++) segs0[(uint32_t)old + j] = Seg{s, rs + j * kSeg};
+    } else {
       aq0[atomicAdd(&ctl->aq_size[0], 1)] = s;
+    }
     atomicAdd(&s_mf, (u64)deg);
     if (visit[s] == ctl->full) atomicAdd(&s_dec, (u64)(t_row_ptr[s + 1] - t_row_ptr[s]));
   }
@@ -163,8 +174,9 @@ __global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ ro
                                                   const int32_t* __restrict__ t_row_ptr,
                                                   const int32_t* __restrict__ t_col, BsCtl* __restrict__ ctl,
                                                   u64* __restrict__ visit, u64* __restrict__ fr,
-                                                  int32_t* __restrict__ aq, const int32_t* __restrict__ ul_static,
-                                                  int32_t ul_static_size, int32_t* __restrict__ ul, int32_t n) {
+                                                  int32_t* __restrict__ aq, Seg* __restrict__ segs, size_t segcap,
+                                                  const int32_t* __restrict__ ul_static, int32_t ul_static_size,
+                                                  int32_t* __restrict__ ul, int32_t n) {
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ u64 s_acc[kBlock / 32][32];
@@ -173,11 +185,11 @@ __global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ ro
   const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n;
   u64* __restrict__ fout = fr + (size_t)(L % 3) * n;
   int32_t* aq_out = aq + (size_t)(L % 3) * n;
-  int32_t* al_out = aq + (size_t)(3 + L % 3) * n;
+  Seg* seg_out = segs + (size_t)(L % 3) * segcap;
   int32_t* aq_count = &ctl->aq_size[L % 3];
-  int32_t* al_count = &ctl->al_size[L % 3];
-  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3]);
-  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)(3 + (L + 1) % 3) * n, ctl->al_size[(L + 1) % 3]);
+  u64* al_pack = &ctl->alpack[L % 3];
+  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
+               segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
   const int cur = ctl->ul_cur;
   const int32_t* ul_in = cur < 0 ? ul_static : ul + (size_t)cur * n;
   const int un = cur < 0 ? ul_static_size : ctl->ul_size[cur];
@@ -244,17 +256,18 @@ __global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ ro
     __syncwarp();
     const u64 nw = active ? (got & ~vis) : 0ull;
     const bool still = active && ((vis | nw) != full);
-    int odeg = 0;
+    int odeg = 0, ors = 0;
     if (nw) {
       visit[u] = vis | nw;
       fout[u] = nw;
-      odeg = row_ptr[u + 1] - row_ptr[u];
+      ors = row_ptr[u];
+      odeg = row_ptr[u + 1] - ors;
       acc.add((u64)odeg, (u64)deg, nw, !still);
     }
     write_new_bits_warp(dist_base, n, batch, u, nw, L);
     const int pos = warp_append(still, ul_count);
     if (still) ul_out[pos] = u;
-    emit_routed(nw != 0ull, u, odeg, aq_out, aq_count, al_out, al_count);
+    emit_routed(nw != 0ull, u, odeg, ors, aq_out, aq_count, seg_out, al_pack);
   }
   acc.flush(ctl, L % 3);
 }
@@ -266,20 +279,20 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
                                                           const int32_t* __restrict__ col, BsCtl* __restrict__ ctl,
                                                           const u64* __restrict__ visit, u64* __restrict__ fr,
                                                           u64* __restrict__ nxt, int32_t* __restrict__ aq,
+                                                          const Seg* __restrict__ segs, size_t segcap,
                                                           int32_t* __restrict__ tq, int32_t n) {
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
-  __shared__ LongTile s_long;
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n;
   const int32_t* aq_in = aq + (size_t)((L - 1) % 3) * n;
-  const int32_t* al_in = aq + (size_t)(3 + (L - 1) % 3) * n;
+  const Seg* seg_in = segs + (size_t)((L - 1) % 3) * segcap;
   const int qn = ctl->aq_size[(L - 1) % 3];
-  const int ln = ctl->al_size[(L - 1) % 3];
-  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3]);
-  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)(3 + (L + 1) % 3) * n, ctl->al_size[(L + 1) % 3]);
+  const int ln = seg_count(ctl->alpack[(L - 1) % 3]);
+  clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
+               segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
   const int wib = threadIdx.x >> 5;
   auto op = [&](int32_t v, int k, bool valid) {
     bool first = false;
@@ -293,7 +306,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
     const int pos = warp_append(first, &ctl->tq_size);
     if (first) tq[pos] = u;
   };
-  grid_expand_long(row_ptr, al_in, ln, s_long, op);
+  seg_expand(row_ptr, seg_in, ln, op);
   warp_expand(row_ptr, aq_in, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
 }
 
@@ -302,13 +315,13 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
                                                          const int32_t* __restrict__ t_row_ptr,
                                                          BsCtl* __restrict__ ctl, u64* __restrict__ visit,
                                                          u64* __restrict__ fr, u64* __restrict__ nxt,
-                                                         int32_t* __restrict__ aq, const int32_t* __restrict__ tq,
-                                                         int32_t n) {
+                                                         int32_t* __restrict__ aq, Seg* __restrict__ segs,
+                                                         size_t segcap, const int32_t* __restrict__ tq, int32_t n) {
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   u64* __restrict__ fout = fr + (size_t)(L % 3) * n;
   int32_t* aq_out = aq + (size_t)(L % 3) * n;
-  int32_t* al_out = aq + (size_t)(3 + L % 3) * n;
+  Seg* seg_out = segs + (size_t)(L % 3) * segcap;
   const u64 full = ctl->full;
   const int batch = ctl->batch;
   int32_t* dist_base = ctl->dist_base;
@@ -319,7 +332,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
     const int i = base + threadIdx.x;
     u64 nw = 0;
     int32_t u = -1;
-    int odeg = 0;
+    int odeg = 0, ors = 0;
     if (i < tn) {
       u = tq[i];
       const u64 x = nxt[u];
@@ -329,12 +342,13 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
       if (nw) {
         visit[u] = vis | nw;
         fout[u] = nw;
-        odeg = row_ptr[u + 1] - row_ptr[u];
+        ors = row_ptr[u];
+        odeg = row_ptr[u + 1] - ors;
         acc.add((u64)odeg, (u64)(t_row_ptr[u + 1] - t_row_ptr[u]), nw, (vis | nw) == full);
       }
     }
     write_new_bits_warp(dist_base, n, batch, u, nw, L);
-    emit_routed(nw != 0ull, u, odeg, aq_out, &ctl->aq_size[L % 3], al_out, &ctl->al_size[L % 3]);
+    emit_routed(nw != 0ull, u, odeg, ors, aq_out, &ctl->aq_size[L % 3], seg_out, &ctl->alpack[L % 3]);
   }
   acc.flush(ctl, L % 3);
 }
@@ -356,7 +370,7 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphCondition
   ctl->mu -= ctl->mu_dec;
   ctl->mu_dec = 0;
   ctl->tq_size = 0;
-  const int nf = ctl->aq_size[L % 3] + ctl->al_size[L % 3];
+  const int nf = ctl->aq_size[L % 3] + long_vertices(ctl->alpack[L % 3]);
   if (nf == 0 || L >= n) {
     ctl->done = 1;
     if (in_graph) cudaGraphSetConditional(loop, 0);
@@ -364,7 +378,7 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphCondition
   }
   // Level L+1 writes list (L+1)%3, whose stale frontier words level L cleared.
   ctl->aq_size[(L + 1) % 3] = 0;
-  ctl->al_size[(L + 1) % 3] = 0;
+  ctl->alpack[(L + 1) % 3] = 0;
   ctl->mf[(L + 1) % 3] = 0;
   int mode;
   if (ctl->policy == DAWN_VARIANT_PUSH)
@@ -390,7 +404,7 @@ void probe_bs(const void* p, LevelProbe* out) {
   out->level = c->level;
   out->mode = c->mode;
   out->done = c->done;
-  out->frontier = c->aq_size[pin] + c->al_size[pin];
+  out->frontier = c->aq_size[pin] + (int64_t)(c->alpack[pin] >> 32);
   out->frontier_edges = (int64_t)c->mf[pin];
   out->unvisited_edges = c->mu;
 }
@@ -437,9 +451,11 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   const int32_t n = g->n;
   const size_t nn = (size_t)n;
   DAWN_CHECK(build_static_list(g));
-  // words: visit | fr[3] | nxt ; lists: aq[3] | al[3] | tq | ul[2]
+  // words: visit | fr[3] | nxt ; lists: aq[3] | tq | ul[2] ; segments[3]
   DAWN_CHECK(ensure(g->bs_words, sizeof(u64) * 5 * nn));
-  DAWN_CHECK(ensure(g->bs_queues, sizeof(int32_t) * 9 * nn));
+  DAWN_CHECK(ensure(g->bs_queues, sizeof(int32_t) * 6 * nn));
+  const size_t segcap = seg_capacity(n, g->m);
+  DAWN_CHECK(ensure(g->bs_segs, sizeof(Seg) * 3 * segcap));
   DAWN_CHECK(ensure(g->bs_ctl, sizeof(BsCtl)));
   DAWN_CHECK(ensure(g->bs_sources, sizeof(int32_t) * (size_t)nsrc));
   DAWN_CUDA(cudaMemcpyAsync(g->bs_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
@@ -458,6 +474,8 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
     const int32_t *row_ptr, *col, *t_row_ptr, *t_col, *ul_static;
     u64 *words, *visit, *fr, *fr0, *nxt;
     int32_t *aq, *aq0, *tq, *ul;
+    Seg* segs;
+    size_t segcap;
     int32_t ul_static_size;
     size_t nwords;
     int32_t n;
@@ -479,19 +497,23 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   a.nxt = a.words + 4 * nn;
   a.aq = g->bs_queues.as<int32_t>();
   a.aq0 = a.aq;
-  a.tq = a.aq + 6 * nn;
-  a.ul = a.aq + 7 * nn;
+  a.tq = a.aq + 3 * nn;
+  a.ul = a.aq + 4 * nn;
+  a.segs = g->bs_segs.as<Seg>();
+  a.segcap = segcap;
   a.nwords = 5 * nn;
   a.n = n;
   a.m = g->m;
   a.handle = 0;
   a.in_graph = 0;
   void* clear_args[] = {&a.words, &a.nwords};
-  void* init_args[] = {&a.ctl, &a.row_ptr, &a.t_row_ptr, &a.visit, &a.fr0, &a.aq0, &a.n, &a.m};
-  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.aq,
-                       &a.ul_static, &a.ul_static_size, &a.ul, &a.n};
-  void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.tq, &a.n};
-  void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.tq, &a.n};
+  void* init_args[] = {&a.ctl, &a.row_ptr, &a.t_row_ptr, &a.visit, &a.fr0, &a.aq0, &a.segs, &a.n, &a.m};
+  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.aq, &a.segs,
+                       &a.segcap, &a.ul_static, &a.ul_static_size, &a.ul, &a.n};
+  void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.segs, &a.segcap,
+                          &a.tq, &a.n};
+  void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.segs,
+                         &a.segcap, &a.tq, &a.n};
   void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
   const int sms = g->geo.sms;
