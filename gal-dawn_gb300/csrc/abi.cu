@@ -196,8 +196,9 @@ dawn_status staged(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* ho
     const int32_t c = nsrc - i0 < chunk ? nsrc - i0 : chunk;
     dawn_stats s;
     DAWN_CHECK(run(sources + i0, c, g->dist_stage.p, st ? &s : nullptr));
-    DAWN_CUDA(cudaMemcpyAsync(static_cast<char*>(host_dist) + row_bytes * (size_t)i0, g->dist_stage.p,
-                              row_bytes * (size_t)c, cudaMemcpyDeviceToHost, g->stream));
+    if (host_dist)
+      DAWN_CUDA(cudaMemcpyAsync(static_cast<char*>(host_dist) + row_bytes * (size_t)i0, g->dist_stage.p,
+                                row_bytes * (size_t)c, cudaMemcpyDeviceToHost, g->stream));
     if (st) add_stats(st, s);
   }
   DAWN_CUDA(cudaStreamSynchronize(g->stream));
@@ -323,8 +324,8 @@ dawn_status dawn_bfs_device(dawn_graph* g, const int32_t* sources, int32_t nsrc,
 dawn_status dawn_bfs(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* dist, int32_t variant,
                      dawn_stats* stats) {
   dawn::clear_error();
-  if (!g || (nsrc > 0 && !dist)) {
-    dawn::set_error("graph or distance buffer is NULL");
+  if (!g) {
+    dawn::set_error("graph is NULL");
     return DAWN_ERR_INVALID_ARG;
   }
   DAWN_CHECK(check_sources(g, sources, nsrc));
@@ -362,8 +363,8 @@ dawn_status dawn_sssp(dawn_graph* g, const int32_t* sources, int32_t nsrc, void*
                       dawn_stats* stats) {
   dawn::clear_error();
   (void)variant;
-  if (!g || (nsrc > 0 && !dist)) {
-    dawn::set_error("graph or distance buffer is NULL");
+  if (!g) {
+    dawn::set_error("graph is NULL");
     return DAWN_ERR_INVALID_ARG;
   }
   if (g->wtype == DAWN_W_NONE) {

@@ -1,0 +1,12 @@
+// Single-source weighted shortest paths on the GPU, API of
+// include/dawn/algorithm/gpu/sssp.cuh in the reference project.
+#pragma once
+#include <dawn/dawn.cuh>
+
+namespace DAWN {
+namespace SSSP_GPU {
+
+float run(Graph::Graph_t& graph, std::string& output_path);
+
+}  // namespace SSSP_GPU
+}  // namespace DAWN

@@ -1,0 +1,5 @@
+// GPU-side umbrella header.  The algorithms behind it run on the GB300
+// kernels of libdawn_gb300.so through the C ABI (dawn_gb300.h); no CUDA or
+// Thrust type appears in this API, so callers build with a plain C++ compiler.
+#pragma once
+#include <dawn/dawn.hxx>

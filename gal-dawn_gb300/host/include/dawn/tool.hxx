@@ -1,0 +1,13 @@
+// Small helpers, API of include/dawn/tool.hxx in the reference project.
+#pragma once
+#include <dawn/include.hxx>
+
+namespace DAWN {
+namespace Tool {
+
+float average(int* result, int n);
+float average(float* result, int n);
+void infoprint(int entry, int total, int interval, int thread, float elapsed_time);
+
+}  // namespace Tool
+}  // namespace DAWN

@@ -99,7 +99,9 @@ dawn_status dawn_graph_synchronize(dawn_graph* g);
  * (src/algorithm/gpu/mssp.cu:9-51) and APSP_GPU::run
  * (src/algorithm/gpu/apsp.cu:62-111) for many.  Sources must lie in [0, n);
  * isolated sources are legal (their row holds only the 0 at the source).
- * stats may be NULL. */
+ * dist may be NULL: the traversal runs and only the statistics come back
+ * (the reference's MSSP/APSP drivers discard the distances the same way
+ * unless printing).  stats may be NULL. */
 dawn_status dawn_bfs(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                      int32_t* dist, int32_t variant, dawn_stats* stats);
 
@@ -114,7 +116,8 @@ dawn_status dawn_bfs_device(dawn_graph* g, const int32_t* sources,
  * SSSP_GPU::kernel + GOVM (src/algorithm/gpu/sssp.cu:18-129) and
  * MSSP_GPU::run_Weighted (src/algorithm/gpu/mssp.cu:53-102).  The source's
  * own row initialises its neighbours with the last CSR entry of a repeated
- * neighbour, as the reference CPU path does (src/algorithm/cpu/sssp.cpp:41-45). */
+ * neighbour, as the reference CPU path does (src/algorithm/cpu/sssp.cpp:41-45).
+ * As with dawn_bfs, a NULL dist returns only the statistics. */
 dawn_status dawn_sssp(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                       void* dist, int32_t variant, dawn_stats* stats);
 dawn_status dawn_sssp_device(dawn_graph* g, const int32_t* sources,
