@@ -261,6 +261,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--quick", action="store_true",
+                    help="only the device-resident timing (profiling runs); prints a short JSON line")
+    ap.add_argument("--traced", action="store_true",
+                    help="with --quick: run the steps level by level, launching only the kernels each level uses")
+    ap.add_argument("--variant", default="bitset", choices=["bitset", "do", "push"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -285,6 +290,20 @@ def main():
 
     dg = abi.Graph(g, stream=stream)
     d_dist = torch.empty((NSRC, g.n), dtype=torch.int32, device="cuda")
+    if args.quick:
+        var = {"bitset": abi.VARIANT_BITSET, "do": abi.VARIANT_DO, "push": abi.VARIANT_PUSH}[args.variant]
+        dg.trace(args.traced)
+        quick = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=False)  # noqa: E731
+        ms = time_steps(torch, quick, args.steps, args.warmup, barrier) / max(1, args.steps)
+        recs = dg.trace_read() if args.traced else []
+        st = dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=True)
+        if rank == 0:
+            print(json.dumps({"quick": True, "variant": args.variant, "traced": args.traced, "scale": args.scale,
+                              "ms_per_step": round(ms, 4), "edges": st.edges_traversed,
+                              "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2),
+                              "kernels": len(recs)}), flush=True)
+        dg.close()
+        return
     step = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=False)  # noqa
     st = dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=True)
     edges = st.edges_traversed
