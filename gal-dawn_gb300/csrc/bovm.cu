@@ -298,7 +298,8 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   fam.body[1] = {(const void*)bfs_pull, pull_args, dim3(persistent_blocks((const void*)bfs_pull, kBlock, 0)),
                  dim3(kBlock), "bfs_pull", kModePull};
   fam.body[2] = {(const void*)bfs_decide, decide_args, dim3(1), dim3(32), "bfs_decide"};
-  fam.post = {(const void*)ss_next, next_args, dim3(1), dim3(32), "ss_next"};
+  fam.npost = 1;
+  fam.post[0] = {(const void*)ss_next, next_args, dim3(1), dim3(32), "ss_next"};
   fam.ctl = a.ctl;
   fam.ctl_bytes = sizeof(SsCtl);
   fam.probe = probe_ss;

@@ -80,7 +80,7 @@ struct SsCtl {
 
 // Kernel launches of one frontier-traversal family.  The driver runs them as
 // one CUDA graph per source (or per source batch):
-//   pre[0] -> ... -> while(cond){ body[0] -> ... -> body[nbody-1] } -> post
+//   pre[0] -> ... -> while(cond){ body[0] -> ... -> body[nbody-1] } -> post[0] -> ...
 // where the last body kernel ("decide") ends the loop through
 // cudaGraphSetConditional.  When conditional graphs are unavailable the
 // same sequence runs from a host loop that polls the `done` word.
@@ -103,7 +103,8 @@ struct SsFamily {
   int npre = 0;
   Launch body[5];
   int nbody = 0;
-  Launch post;
+  Launch post[2];
+  int npost = 0;
   // the decide kernel (body[nbody-1]) takes these two arguments
   cudaGraphConditionalHandle* handle = nullptr;
   int* in_graph = nullptr;

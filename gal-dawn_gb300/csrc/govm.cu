@@ -247,7 +247,8 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   fam.body[0] = {(const void*)sssp_relax, relax_args,
                  dim3(persistent_blocks((const void*)sssp_relax, kBlock, 0)), dim3(kBlock), "sssp_relax"};
   fam.body[1] = {(const void*)sssp_decide, decide_args, dim3(1), dim3(32), "sssp_decide"};
-  fam.post = {(const void*)sssp_next, next_args, dim3(1), dim3(32), "sssp_next"};
+  fam.npost = 1;
+  fam.post[0] = {(const void*)sssp_next, next_args, dim3(1), dim3(32), "sssp_next"};
   fam.ctl = a.ctl;
   fam.ctl_bytes = sizeof(SsCtl);
   fam.probe = probe_sssp;

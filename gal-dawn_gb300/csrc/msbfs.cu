@@ -17,7 +17,11 @@
 //   push: the active vertices' rows are dealt to warps; new bits are
 //         atomicOr-ed into `next`, the first toucher queues the target, and
 //         an update pass folds `next` into visited / frontier.
-// Both write each new (source, vertex) distance exactly once.
+// Neither writes distances during the traversal: the level at which a bit
+// first appears is recorded in bit-sliced level words (slice k holds bit k
+// of the level of every (source, vertex) pair, 64 sources per word), and a
+// final pass expands them into the nsrc x n distance block with full-line
+// coalesced stores, writing -1 for pairs never reached.
 #include "dawn_device.cuh"
 
 namespace dawn {
@@ -32,7 +36,10 @@ struct BsCtl {
   int32_t ul_cur;              // list the next pull reads: -1 = the graph's static list
   int32_t level, mode, done, policy, batch, nsrc, n_push, n_pull;
   int32_t push_ratio;          // push while push_ratio * frontier edges < unfinished edges
-  int32_t pad;
+  int32_t work;                // dynamic work counter of the current level
+  int32_t dense;               // push level: fire-and-forget scatter + dense update sweep
+  int32_t nbits;               // level slices available
+  int32_t pad3;
   unsigned long long mf[3];    // out-degree sums of the active lists
   long long mu;                // in-degree sum of vertices not yet finished
   long long mu_dec;            // in-degree of vertices finished this level
@@ -52,18 +59,26 @@ __device__ __forceinline__ u64 warp_or64(u64 x) {
   return ((u64)hi << 32) | lo;
 }
 
-// Warp-synchronous form: every lane walks the warp's union of new bits in
-// the same order, so each step stores one distance row's entries for the
-// warp's 32 vertices together.  All lanes must call it.
-__device__ __forceinline__ void write_new_bits_warp(int32_t* __restrict__ dist_base, int32_t n, int batch,
-                                                    int32_t u, u64 nw, int32_t level) {
-  u64 wm = warp_or64(nw);
-  const size_t base = (size_t)batch * 64;
-  while (wm) {
-    const int b = __ffsll((long long)wm) - 1;
-    wm &= wm - 1;
-    if ((nw >> b) & 1ull) dist_base[(base + b) * (size_t)n + u] = level;
+constexpr int kSlicesCleared = 8;  // slices zeroed per batch; higher ones on first use
+
+// Records the level of newly reached (source, vertex) pairs: slice k of
+// vertex u gains nw for every set bit k of the level.  The caller owns u.
+__device__ __forceinline__ void record_level(u64* __restrict__ slices, int32_t n, int32_t u, u64 nw, int32_t level) {
+  for (unsigned L = (unsigned)level; L; L &= L - 1) {
+    u64* w = slices + (size_t)(__ffs(L) - 1) * n + u;
+    *w |= nw;
   }
+}
+
+// Level L is the last one before slice log2(L + 1) is first used: clear it.
+__device__ __forceinline__ void clear_next_slice(u64* __restrict__ slices, int32_t n, int32_t level, int nbits) {
+  const unsigned next = (unsigned)level + 1;
+  if (next & (next - 1)) return;
+  const int b = __ffs(next) - 1;
+  if (b < kSlicesCleared || b >= nbits) return;
+  u64* w = slices + (size_t)b * n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride) w[i] = 0ull;
 }
 
 // Zero the frontier words listed in a stale active list and its segment
@@ -103,6 +118,8 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     ctl->ul_size[0] = 0;
     ctl->ul_size[1] = 0;
     ctl->ul_cur = -1;
+    ctl->work = 0;
+    ctl->dense = 0;
     ctl->full = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
   }
   __syncthreads();
@@ -113,7 +130,6 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     const u64 bit = 1ull << b;
     atomicOr(visit + s, bit);
     first = atomicOr(fr0 + s, bit) == 0ull;
-    ctl->dist_base[((size_t)batch * 64 + b) * (size_t)n + s] = 0;
     atomicAdd(&s_reached, (u64)(row_ptr[s + 1] - row_ptr[s]));
   }
   __syncthreads();
@@ -170,13 +186,14 @@ struct LevelAcc {
 // concatenated across the warp and OR-ed into per-lane shared-memory slots.
 // The vertex then owns its words: no global atomics.  The list is filtered
 // into the next unfinished list as it goes.
-__global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ row_ptr,
-                                                  const int32_t* __restrict__ t_row_ptr,
-                                                  const int32_t* __restrict__ t_col, BsCtl* __restrict__ ctl,
-                                                  u64* __restrict__ visit, u64* __restrict__ fr,
-                                                  int32_t* __restrict__ aq, Seg* __restrict__ segs, size_t segcap,
-                                                  const int32_t* __restrict__ ul_static, int32_t ul_static_size,
-                                                  int32_t* __restrict__ ul, int32_t n) {
+__global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__ row_ptr,
+                                                     const int32_t* __restrict__ t_row_ptr,
+                                                     const int32_t* __restrict__ t_col, BsCtl* __restrict__ ctl,
+                                                     u64* __restrict__ visit, u64* __restrict__ fr,
+                                                     u64* __restrict__ slices, int32_t* __restrict__ aq,
+                                                     Seg* __restrict__ segs, size_t segcap,
+                                                     const int32_t* __restrict__ ul_static, int32_t ul_static_size,
+                                                     int32_t* __restrict__ ul, int32_t n) {
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ u64 s_acc[kBlock / 32][32];
@@ -190,6 +207,7 @@ __global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ ro
   u64* al_pack = &ctl->alpack[L % 3];
   clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
                segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
+  clear_next_slice(slices, n, L, ctl->nbits);
   const int cur = ctl->ul_cur;
   const int32_t* ul_in = cur < 0 ? ul_static : ul + (size_t)cur * n;
   const int un = cur < 0 ? ul_static_size : ctl->ul_size[cur];
@@ -197,11 +215,16 @@ __global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ ro
   int32_t* ul_out = ul + (size_t)nxt * n;
   int32_t* ul_count = &ctl->ul_size[nxt];
   const u64 full = ctl->full;
-  const int batch = ctl->batch;
-  int32_t* dist_base = ctl->dist_base;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   LevelAcc acc;
-  for (int base = global_warp() * 32; base < un; base += num_warps() * 32) {
+  // Warps take 32 list entries at a time from a shared counter: the rows
+  // behind the entries differ widely in length, static striding does not
+  // balance them.
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctl->work, 32);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= un) break;
     const int idx = base + lane;
     int32_t u = -1;
     u64 vis = full;
@@ -260,11 +283,11 @@ __global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ ro
     if (nw) {
       visit[u] = vis | nw;
       fout[u] = nw;
+      record_level(slices, n, u, nw, L);
       ors = row_ptr[u];
       odeg = row_ptr[u + 1] - ors;
       acc.add((u64)odeg, (u64)deg, nw, !still);
     }
-    write_new_bits_warp(dist_base, n, batch, u, nw, L);
     const int pos = warp_append(still, ul_count);
     if (still) ul_out[pos] = u;
     emit_routed(nw != 0ull, u, odeg, ors, aq_out, aq_count, seg_out, al_pack);
@@ -272,15 +295,18 @@ __global__ void __launch_bounds__(kBlock) bs_pull(const int32_t* __restrict__ ro
   acc.flush(ctl, L % 3);
 }
 
-// Push, phase 1: the active vertices' rows are dealt to warps; bits new to a
-// target are atomicOr-ed into `next` (skipped when `next` already holds
-// them), and the first toucher queues the target.
+// Push, phase 1: the active vertices' rows (short rows warp-cooperatively,
+// long rows as segments) are dealt to warps; bits new to a target are
+// atomicOr-ed into `next` unless `next` already holds them.  In list mode
+// the first toucher (old word 0) queues the target for phase 2; in dense
+// mode (large frontiers) the atomic result is not needed and phase 2 sweeps
+// all vertices instead.
 __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restrict__ row_ptr,
                                                           const int32_t* __restrict__ col, BsCtl* __restrict__ ctl,
                                                           const u64* __restrict__ visit, u64* __restrict__ fr,
-                                                          u64* __restrict__ nxt, int32_t* __restrict__ aq,
-                                                          const Seg* __restrict__ segs, size_t segcap,
-                                                          int32_t* __restrict__ tq, int32_t n) {
+                                                          u64* __restrict__ nxt, u64* __restrict__ slices,
+                                                          int32_t* __restrict__ aq, const Seg* __restrict__ segs,
+                                                          size_t segcap, int32_t* __restrict__ tq, int32_t n) {
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
@@ -291,8 +317,10 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
   const Seg* seg_in = segs + (size_t)((L - 1) % 3) * segcap;
   const int qn = ctl->aq_size[(L - 1) % 3];
   const int ln = seg_count(ctl->alpack[(L - 1) % 3]);
+  const bool dense = ctl->dense != 0;
   clear_listed(fr + (size_t)((L + 1) % 3) * n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
                segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
+  clear_next_slice(slices, n, L, ctl->nbits);
   const int wib = threadIdx.x >> 5;
   auto op = [&](int32_t v, int k, bool valid) {
     bool first = false;
@@ -301,31 +329,39 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
       u = __ldg(col + k);
       u64 bits = __ldg(fin + v) & ~__ldcg(visit + u);
       if (bits) bits &= ~__ldcg(nxt + u);
-      if (bits) first = atomicOr(nxt + u, bits) == 0ull;
+      if (bits) {
+        if (dense)
+          atomicOr(nxt + u, bits);
+        else
+          first = atomicOr(nxt + u, bits) == 0ull;
+      }
     }
-    const int pos = warp_append(first, &ctl->tq_size);
-    if (first) tq[pos] = u;
+    if (!dense) {
+      const int pos = warp_append(first, &ctl->tq_size);
+      if (first) tq[pos] = u;
+    }
   };
   seg_expand(row_ptr, seg_in, ln, op);
   warp_expand(row_ptr, aq_in, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
 }
 
-// Push, phase 2: fold `next` into visited / frontier for the touched vertices.
+// Push, phase 2: fold `next` into visited / frontier / level slices, over
+// the touched list (list mode) or over every vertex (dense mode).
 __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restrict__ row_ptr,
                                                          const int32_t* __restrict__ t_row_ptr,
                                                          BsCtl* __restrict__ ctl, u64* __restrict__ visit,
                                                          u64* __restrict__ fr, u64* __restrict__ nxt,
-                                                         int32_t* __restrict__ aq, Seg* __restrict__ segs,
-                                                         size_t segcap, const int32_t* __restrict__ tq, int32_t n) {
+                                                         u64* __restrict__ slices, int32_t* __restrict__ aq,
+                                                         Seg* __restrict__ segs, size_t segcap,
+                                                         const int32_t* __restrict__ tq, int32_t n) {
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   u64* __restrict__ fout = fr + (size_t)(L % 3) * n;
   int32_t* aq_out = aq + (size_t)(L % 3) * n;
   Seg* seg_out = segs + (size_t)(L % 3) * segcap;
   const u64 full = ctl->full;
-  const int batch = ctl->batch;
-  int32_t* dist_base = ctl->dist_base;
-  const int tn = ctl->tq_size;
+  const bool dense = ctl->dense != 0;
+  const int tn = dense ? n : ctl->tq_size;
   LevelAcc acc;
   const int total = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < tn; base += total) {
@@ -334,23 +370,52 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
     int32_t u = -1;
     int odeg = 0, ors = 0;
     if (i < tn) {
-      u = tq[i];
+      u = dense ? i : tq[i];
       const u64 x = nxt[u];
-      nxt[u] = 0ull;
-      const u64 vis = visit[u];
-      nw = x & ~vis;
-      if (nw) {
-        visit[u] = vis | nw;
-        fout[u] = nw;
-        ors = row_ptr[u];
-        odeg = row_ptr[u + 1] - ors;
-        acc.add((u64)odeg, (u64)(t_row_ptr[u + 1] - t_row_ptr[u]), nw, (vis | nw) == full);
+      if (x) {
+        nxt[u] = 0ull;
+        const u64 vis = visit[u];
+        nw = x & ~vis;
+        if (nw) {
+          visit[u] = vis | nw;
+          fout[u] = nw;
+          record_level(slices, n, u, nw, L);
+          ors = row_ptr[u];
+          odeg = row_ptr[u + 1] - ors;
+          acc.add((u64)odeg, (u64)(t_row_ptr[u + 1] - t_row_ptr[u]), nw, (vis | nw) == full);
+        }
       }
     }
-    write_new_bits_warp(dist_base, n, batch, u, nw, L);
     emit_routed(nw != 0ull, u, odeg, ors, aq_out, &ctl->aq_size[L % 3], seg_out, &ctl->alpack[L % 3]);
   }
   acc.flush(ctl, L % 3);
+}
+
+// Expands the level slices of one batch into its distance rows: thread per
+// vertex, one store per source, consecutive vertices per warp (full lines).
+__global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__ ctl, const u64* __restrict__ visit,
+                                                       const u64* __restrict__ slices, int32_t n) {
+  const int batch = ctl->batch;
+  const int nb = min(64, ctl->nsrc - batch * 64);
+  const int nbits = 32 - __clz(max(ctl->level, 1));
+  int32_t* dist = ctl->dist_base + (size_t)batch * 64 * n;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < (size_t)n; u += stride) {
+    const u64 vis = visit[u];
+    u64 w[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) w[k] = k < nbits ? slices[(size_t)k * n + u] : 0ull;
+    for (int s = 0; s < nb; s++) {
+      int32_t v = -1;
+      if ((vis >> s) & 1ull) {
+        v = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) v |= (int32_t)((w[k] >> s) & 1ull) << k;
+        for (int k = 8; k < nbits; k++) v |= (int32_t)((slices[(size_t)k * n + u] >> s) & 1ull) << k;
+      }
+      dist[(size_t)s * n + u] = v;
+    }
+  }
 }
 
 __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop, int in_graph) {
@@ -370,6 +435,7 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphCondition
   ctl->mu -= ctl->mu_dec;
   ctl->mu_dec = 0;
   ctl->tq_size = 0;
+  ctl->work = 0;
   const int nf = ctl->aq_size[L % 3] + long_vertices(ctl->alpack[L % 3]);
   if (nf == 0 || L >= n) {
     ctl->done = 1;
@@ -385,6 +451,9 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphCondition
     mode = kModePush;
   else
     mode = (long long)ctl->mf[L % 3] * ctl->push_ratio < ctl->mu ? kModePush : kModePull;
+  // A push whose frontier edges reach n/16 touches enough vertices that a
+  // dense update sweep beats queueing every first touch.
+  ctl->dense = (long long)ctl->mf[L % 3] * 16 >= (long long)n;
   ctl->mode = mode;
   ctl->level = L + 1;
 }
@@ -451,8 +520,9 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   const int32_t n = g->n;
   const size_t nn = (size_t)n;
   DAWN_CHECK(build_static_list(g));
-  // words: visit | fr[3] | nxt ; lists: aq[3] | tq | ul[2] ; segments[3]
-  DAWN_CHECK(ensure(g->bs_words, sizeof(u64) * 5 * nn));
+  // words: visit | fr[3] | nxt | level slices[nbits] ; lists: aq[3] | tq | ul[2] ; segments[3]
+  const int nbits = 32 - __builtin_clz((unsigned)n);  // levels never exceed n
+  DAWN_CHECK(ensure(g->bs_words, sizeof(u64) * (5 + (size_t)nbits) * nn));
   DAWN_CHECK(ensure(g->bs_queues, sizeof(int32_t) * 6 * nn));
   const size_t segcap = seg_capacity(n, g->m);
   DAWN_CHECK(ensure(g->bs_segs, sizeof(Seg) * 3 * segcap));
@@ -460,11 +530,11 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   DAWN_CHECK(ensure(g->bs_sources, sizeof(int32_t) * (size_t)nsrc));
   DAWN_CUDA(cudaMemcpyAsync(g->bs_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
                             g->stream));
-  DAWN_CUDA(cudaMemsetAsync(d_dist, 0xff, sizeof(int32_t) * (size_t)nsrc * nn, g->stream));
   BsCtl c = {};
   c.nsrc = nsrc;
   c.policy = DAWN_VARIANT_BITSET;
   c.push_ratio = g->bs_push_ratio;
+  c.nbits = nbits;
   c.dist_base = d_dist;
   c.sources = g->bs_sources.as<int32_t>();
   DAWN_CUDA(cudaMemcpyAsync(g->bs_ctl.p, &c, sizeof(BsCtl), cudaMemcpyHostToDevice, g->stream));
@@ -472,7 +542,7 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   struct {
     BsCtl* ctl;
     const int32_t *row_ptr, *col, *t_row_ptr, *t_col, *ul_static;
-    u64 *words, *visit, *fr, *fr0, *nxt;
+    u64 *words, *visit, *fr, *fr0, *nxt, *slices;
     int32_t *aq, *aq0, *tq, *ul;
     Seg* segs;
     size_t segcap;
@@ -495,25 +565,27 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   a.fr = a.words + nn;
   a.fr0 = a.fr;
   a.nxt = a.words + 4 * nn;
+  a.slices = a.words + 5 * nn;
   a.aq = g->bs_queues.as<int32_t>();
   a.aq0 = a.aq;
   a.tq = a.aq + 3 * nn;
   a.ul = a.aq + 4 * nn;
   a.segs = g->bs_segs.as<Seg>();
   a.segcap = segcap;
-  a.nwords = 5 * nn;
+  a.nwords = (5 + (size_t)(nbits < kSlicesCleared ? nbits : kSlicesCleared)) * nn;
   a.n = n;
   a.m = g->m;
   a.handle = 0;
   a.in_graph = 0;
   void* clear_args[] = {&a.words, &a.nwords};
   void* init_args[] = {&a.ctl, &a.row_ptr, &a.t_row_ptr, &a.visit, &a.fr0, &a.aq0, &a.segs, &a.n, &a.m};
-  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.aq, &a.segs,
+  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.slices, &a.aq, &a.segs,
                        &a.segcap, &a.ul_static, &a.ul_static_size, &a.ul, &a.n};
-  void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.segs, &a.segcap,
-                          &a.tq, &a.n};
-  void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.aq, &a.segs,
+  void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
+                          &a.segcap, &a.tq, &a.n};
+  void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
                          &a.segcap, &a.tq, &a.n};
+  void* emit_args[] = {&a.ctl, &a.visit, &a.slices, &a.n};
   void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
   const int sms = g->geo.sms;
@@ -531,7 +603,9 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
                  dim3(persistent_blocks((const void*)bs_push_update, kBlock, 0)), dim3(kBlock),
                  "bs_push_update", kModePush};
   fam.body[3] = {(const void*)bs_decide, decide_args, dim3(1), dim3(32), "bs_decide"};
-  fam.post = {(const void*)bs_next, next_args, dim3(1), dim3(32), "bs_next"};
+  fam.npost = 2;
+  fam.post[0] = {(const void*)bs_emit_dist, emit_args, dim3(sms * 8), dim3(kBlock), "bs_emit_dist"};
+  fam.post[1] = {(const void*)bs_next, next_args, dim3(1), dim3(32), "bs_next"};
   fam.ctl = a.ctl;
   fam.ctl_bytes = sizeof(BsCtl);
   fam.probe = probe_bs;

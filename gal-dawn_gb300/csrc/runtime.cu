@@ -114,7 +114,12 @@ dawn_status build_graph(SsFamily& fam, cudaGraphExec_t* exec) {
       bprev = node;
     }
     if (st != DAWN_OK) break;
-    if ((st = add_kernel(graph, &node, &loop, fam.post)) != DAWN_OK) break;
+    cudaGraphNode_t pprev = loop;
+    for (int i = 0; i < fam.npost && st == DAWN_OK; i++) {
+      st = add_kernel(graph, &node, &pprev, fam.post[i]);
+      pprev = node;
+    }
+    if (st != DAWN_OK) break;
     e = cudaGraphInstantiate(exec, graph, 0);
     if (e != cudaSuccess) {
       set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
@@ -181,7 +186,7 @@ dawn_status ss_run_traced(dawn_graph* g, SsFamily& fam, int32_t nruns) {
         g->trace_log.push_back(r);
       }
     }
-    DAWN_CHECK(launch(fam.post, g->stream));
+    for (int j = 0; j < fam.npost; j++) DAWN_CHECK(launch(fam.post[j], g->stream));
   }
   return DAWN_OK;
 }
@@ -212,7 +217,7 @@ dawn_status ss_run(dawn_graph* g, SsFamily& fam, int32_t nruns, cudaGraphExec_t*
       DAWN_CUDA(cudaStreamSynchronize(g->stream));
       if (*h_done) break;
     }
-    DAWN_CHECK(launch(fam.post, g->stream));
+    for (int j = 0; j < fam.npost; j++) DAWN_CHECK(launch(fam.post[j], g->stream));
   }
   return DAWN_OK;
 }
