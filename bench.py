@@ -146,6 +146,8 @@ def bitset_roofline(dg, g, srcs, d_dist, abi, peak_gbs, peak_kind):
             r["unvisited_edges"], r["ms"]))
     per = {}
     for r in recs:
+        if r["kernel"] in ("bs_init", "bs_next"):  # one-thread bookkeeping
+            continue
         k = per.setdefault(r["kernel"], {"launches": 0, "ms": 0.0, "bytes": 0})
         k["launches"] += 1
         k["ms"] += r["ms"]
@@ -182,6 +184,10 @@ def alg_bytes(r, n, m):
         return 4 * (r["frontier"] + r["frontier_edges"])
     if k == "bs_push_update":
         return 24 * min(r["frontier_edges"], n)
+    if k == "bs_emit_dist":
+        return 4 * NSRC * n + 8 * n * 5  # distance block written once + visited and level words read
+    if k == "bs_clear":
+        return 8 * n * 9  # visited, three frontier, next and four level words zeroed
     if k == "bfs_pull":
         return 4 * (n + 1) + n // 8 + 4 * r["unvisited_edges"]
     if k == "bfs_push":

@@ -247,9 +247,19 @@ __global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__
       const int s = __shfl_sync(kFull, rs, leader), e = __shfl_sync(kFull, re, leader);
       const u64 lvis = __shfl_sync(kFull, vis, leader);
       u64 w = 0;
-      for (int k0 = s; k0 < e; k0 += 32) {
+      // Four independent gathers in flight per lane, one early-exit test
+      // per 128 entries.
+      for (int k0 = s; k0 < e; k0 += 128) {
         const int k = k0 + lane;
-        if (k < e) w |= __ldg(fin + __ldg(t_col + k));
+        const int32_t v0 = k < e ? __ldg(t_col + k) : -1;
+        const int32_t v1 = k + 32 < e ? __ldg(t_col + k + 32) : -1;
+        const int32_t v2 = k + 64 < e ? __ldg(t_col + k + 64) : -1;
+        const int32_t v3 = k + 96 < e ? __ldg(t_col + k + 96) : -1;
+        const u64 x0 = v0 >= 0 ? __ldg(fin + v0) : 0ull;
+        const u64 x1 = v1 >= 0 ? __ldg(fin + v1) : 0ull;
+        const u64 x2 = v2 >= 0 ? __ldg(fin + v2) : 0ull;
+        const u64 x3 = v3 >= 0 ? __ldg(fin + v3) : 0ull;
+        w |= x0 | x1 | x2 | x3;
         if ((warp_or64(w) | lvis) == full) break;
       }
       w = warp_or64(w);
@@ -262,17 +272,28 @@ __global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__
     s_rs[wib][lane] = rs;
     s_acc[wib][lane] = 0ull;
     __syncwarp();
-    for (int e0 = 0; e0 < total; e0 += 32) {
-      const int e = e0 + lane;
-      if (e < total) {
-        int lo = 0, hi = 31;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (s_excl[wib][mid] <= e) lo = mid; else hi = mid - 1;
+    // Two edges per lane per pass: both searches and both gathers are
+    // independent, so their latencies overlap.
+    for (int e0 = 0; e0 < total; e0 += 64) {
+      const int ea = e0 + lane, eb = ea + 32;
+      int la = 0, lb = 0;
+      {
+        int lo = 0, hi = 31, lo2 = 0, hi2 = 31;
+#pragma unroll
+        for (int it = 0; it < 5; it++) {
+          const int mid = (lo + hi + 1) >> 1, mid2 = (lo2 + hi2 + 1) >> 1;
+          if (s_excl[wib][mid] <= ea) lo = mid; else hi = mid - 1;
+          if (s_excl[wib][mid2] <= eb) lo2 = mid2; else hi2 = mid2 - 1;
         }
-        const u64 x = __ldg(fin + __ldg(t_col + s_rs[wib][lo] + (e - s_excl[wib][lo])));
-        if (x) atomicOr(&s_acc[wib][lo], x);
+        la = lo;
+        lb = lo2;
       }
+      const int32_t va = ea < total ? __ldg(t_col + s_rs[wib][la] + (ea - s_excl[wib][la])) : -1;
+      const int32_t vb = eb < total ? __ldg(t_col + s_rs[wib][lb] + (eb - s_excl[wib][lb])) : -1;
+      const u64 xa = va >= 0 ? __ldg(fin + va) : 0ull;
+      const u64 xb = vb >= 0 ? __ldg(fin + vb) : 0ull;
+      if (xa) atomicOr(&s_acc[wib][la], xa);
+      if (xb) atomicOr(&s_acc[wib][lb], xb);
     }
     __syncwarp();
     if (sdeg > 0) got = s_acc[wib][lane];
@@ -478,18 +499,27 @@ void probe_bs(const void* p, LevelProbe* out) {
   out->unvisited_edges = c->mu;
 }
 
-// Static pull list: every vertex with an in-edge, in id order.
-__global__ void flag_in_degree(const int32_t* __restrict__ t_row_ptr, int32_t n, int64_t* __restrict__ flags) {
+// Static pull list: every vertex with an in-edge, in descending order of
+// log2(in-degree) and by id within a class.  Heavy rows are taken first,
+// so the last chunks of a pull sweep are light ones and the sweep has no
+// long tail; lists filtered from it keep roughly the same order.
+__device__ __forceinline__ int degree_class(const int32_t* __restrict__ t_row_ptr, int32_t i) {
+  const int d = t_row_ptr[i + 1] - t_row_ptr[i];
+  return d > 0 ? 32 - __clz(d) : 0;  // 1..31, 0 = no in-edge
+}
+
+__global__ void flag_degree_class(const int32_t* __restrict__ t_row_ptr, int32_t n, int cls,
+                                  int64_t* __restrict__ flags) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride)
-    flags[i] = t_row_ptr[i + 1] > t_row_ptr[i] ? 1 : 0;
+    flags[i] = degree_class(t_row_ptr, (int32_t)i) == cls ? 1 : 0;
 }
 
 __global__ void scatter_flagged(const int64_t* __restrict__ flags, const int64_t* __restrict__ pos, int32_t n,
-                                int32_t* __restrict__ out) {
+                                int64_t base, int32_t* __restrict__ out) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride)
-    if (flags[i]) out[pos[i]] = (int32_t)i;
+    if (flags[i]) out[base + pos[i]] = (int32_t)i;
 }
 
 dawn_status build_static_list(dawn_graph* g) {
@@ -499,18 +529,23 @@ dawn_status build_static_list(dawn_graph* g) {
   DAWN_CUDA(cudaMallocAsync(&tmp, sizeof(int64_t) * 2 * ((size_t)n + 1), g->stream));
   int64_t* flags = tmp;
   int64_t* pos = tmp + n + 1;
-  flag_in_degree<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->t_row_ptr, n, flags);
-  DAWN_CUDA(cudaGetLastError());
-  DAWN_CUDA(cudaMemsetAsync(flags + n, 0, sizeof(int64_t), g->stream));
-  DAWN_CHECK(exclusive_scan_i64(flags, pos, (int64_t)n + 1, g->stream));
   DAWN_CHECK(ensure(g->ul_static, sizeof(int32_t) * (size_t)n));
-  scatter_flagged<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(flags, pos, n, g->ul_static.as<int32_t>());
-  DAWN_CUDA(cudaGetLastError());
-  int64_t cnt = 0;
-  DAWN_CUDA(cudaMemcpyAsync(&cnt, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, g->stream));
+  int64_t base = 0;
+  for (int cls = 31; cls >= 1; cls--) {
+    flag_degree_class<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->t_row_ptr, n, cls, flags);
+    DAWN_CUDA(cudaGetLastError());
+    DAWN_CUDA(cudaMemsetAsync(flags + n, 0, sizeof(int64_t), g->stream));
+    DAWN_CHECK(exclusive_scan_i64(flags, pos, (int64_t)n + 1, g->stream));
+    scatter_flagged<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(flags, pos, n, base, g->ul_static.as<int32_t>());
+    DAWN_CUDA(cudaGetLastError());
+    int64_t cnt = 0;
+    DAWN_CUDA(cudaMemcpyAsync(&cnt, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, g->stream));
+    DAWN_CUDA(cudaStreamSynchronize(g->stream));
+    base += cnt;
+  }
   DAWN_CUDA(cudaFreeAsync(tmp, g->stream));
   DAWN_CUDA(cudaStreamSynchronize(g->stream));
-  g->ul_static_size = (int32_t)cnt;
+  g->ul_static_size = (int32_t)base;
   return DAWN_OK;
 }
 

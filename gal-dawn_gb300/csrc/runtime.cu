@@ -154,8 +154,25 @@ dawn_status ss_run_traced(dawn_graph* g, SsFamily& fam, int32_t nruns) {
     int body;
     LevelProbe p;
   };
+  // Times the launches of one stage (pre or post kernels) as level 0 / -1 records.
+  auto timed_stage = [&](const Launch* ls, int cnt, int run, int level) -> dawn_status {
+    for (int j = 0; j < cnt; j++) {
+      DAWN_CUDA(cudaEventRecord(g->trace_ev[0], g->stream));
+      DAWN_CHECK(launch(ls[j], g->stream));
+      DAWN_CUDA(cudaEventRecord(g->trace_ev[1], g->stream));
+      DAWN_CUDA(cudaEventSynchronize(g->trace_ev[1]));
+      dawn_trace_rec r = {};
+      std::snprintf(r.kernel, sizeof(r.kernel), "%s", ls[j].name);
+      r.run = run;
+      r.level = level;
+      r.mode = -1;
+      DAWN_CUDA(cudaEventElapsedTime(&r.ms, g->trace_ev[0], g->trace_ev[1]));
+      g->trace_log.push_back(r);
+    }
+    return DAWN_OK;
+  };
   for (int32_t run = 0; run < nruns; run++) {
-    for (int j = 0; j < fam.npre; j++) DAWN_CHECK(launch(fam.pre[j], g->stream));
+    DAWN_CHECK(timed_stage(fam.pre, fam.npre, run, 0));
     for (;;) {
       DAWN_CUDA(cudaMemcpyAsync(host.data(), fam.ctl, fam.ctl_bytes, cudaMemcpyDeviceToHost, g->stream));
       DAWN_CUDA(cudaStreamSynchronize(g->stream));
@@ -186,7 +203,7 @@ dawn_status ss_run_traced(dawn_graph* g, SsFamily& fam, int32_t nruns) {
         g->trace_log.push_back(r);
       }
     }
-    for (int j = 0; j < fam.npost; j++) DAWN_CHECK(launch(fam.post[j], g->stream));
+    DAWN_CHECK(timed_stage(fam.post, fam.npost, run, -1));
   }
   return DAWN_OK;
 }
