@@ -86,7 +86,7 @@ void destroy(dawn_graph* g) {
   cudaFree(g->col);
   if (g->val) cudaFree(g->val);
   DevBuf* bufs[] = {&g->ss_queues, &g->ss_segs, &g->bs_segs, &g->ss_bitmaps, &g->ss_ctl, &g->ss_sources, &g->ss_scratch,
-                    &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->cc_out,
+                    &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
                     &g->dist_stage};
   for (DevBuf* b : bufs) dawn::release(*b);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);

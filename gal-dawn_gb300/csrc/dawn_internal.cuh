@@ -158,8 +158,12 @@ struct dawn_graph {
   dawn::DevBuf bs_ctl;
   dawn::DevBuf bs_sources;
   dawn::DevBuf bs_segs;         // 3 x seg_capacity long-row segments
-  dawn::DevBuf ul_static;       // vertices with an in-edge (pull work list)
+  dawn::DevBuf ul_static;       // light pull rows: 0 < in-degree < kPullHeavy, id order
   int32_t ul_static_size = 0;
+  dawn::DevBuf hv_static;       // heavy pull rows: in-degree >= kPullHeavy, id order
+  dawn::DevBuf hv_segoff;       // exclusive prefix of their segment counts (nh + 1)
+  dawn::DevBuf hv_acc;          // per heavy row: OR accumulator + finished-segment count
+  int32_t hv_count = 0, hv_segs = 0;
   int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges
 
   // closeness reduction

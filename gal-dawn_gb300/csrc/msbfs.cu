@@ -36,7 +36,8 @@ struct BsCtl {
   int32_t ul_cur;              // list the next pull reads: -1 = the graph's static list
   int32_t level, mode, done, policy, batch, nsrc, n_push, n_pull;
   int32_t push_ratio;          // push while push_ratio * frontier edges < unfinished edges
-  int32_t work;                // dynamic work counter of the current level
+  int32_t work;                // dynamic work counter of the current level (light rows)
+  int32_t hwork;               // dynamic work counter of the heavy-row segments
   int32_t dense;               // push level: fire-and-forget scatter + dense update sweep
   int32_t nbits;               // level slices available
   int32_t pad3;
@@ -59,7 +60,9 @@ __device__ __forceinline__ u64 warp_or64(u64 x) {
   return ((u64)hi << 32) | lo;
 }
 
-constexpr int kSlicesCleared = 8;  // slices zeroed per batch; higher ones on first use
+constexpr int kSlicesCleared = 8;
+constexpr int kPullHeavy = 2048;  // in-degree from which a pull row is cut into segments
+constexpr int kPullSeg = 1024;    // entries per heavy-row segment  // slices zeroed per batch; higher ones on first use
 
 // Records the level of newly reached (source, vertex) pairs: slice k of
 // vertex u gains nw for every set bit k of the level.  The caller owns u.
@@ -119,6 +122,7 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     ctl->ul_size[1] = 0;
     ctl->ul_cur = -1;
     ctl->work = 0;
+    ctl->hwork = 0;
     ctl->dense = 0;
     ctl->full = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
   }
@@ -193,7 +197,9 @@ __global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__
                                                      u64* __restrict__ slices, int32_t* __restrict__ aq,
                                                      Seg* __restrict__ segs, size_t segcap,
                                                      const int32_t* __restrict__ ul_static, int32_t ul_static_size,
-                                                     int32_t* __restrict__ ul, int32_t n) {
+                                                     int32_t* __restrict__ ul, const int32_t* __restrict__ hv_static,
+                                                     const int32_t* __restrict__ hv_segoff, u64* __restrict__ hv_acc,
+                                                     int32_t hv_count, int32_t hv_segs, int32_t n) {
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ u64 s_acc[kBlock / 32][32];
@@ -217,9 +223,73 @@ __global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__
   const u64 full = ctl->full;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   LevelAcc acc;
-  // Warps take 32 list entries at a time from a shared counter: the rows
-  // behind the entries differ widely in length, static striding does not
-  // balance them.
+  // Heavy rows first, one kPullSeg-entry segment per warp task.  Each
+  // segment ORs its gathers into the row's accumulator; the warp finishing
+  // the row's last segment folds the accumulator into the vertex.  Only
+  // that warp writes the vertex's words, so every segment sees the same
+  // visited word for the whole level.
+  for (;;) {
+    int sidx = 0;
+    if (lane == 0) sidx = atomicAdd(&ctl->hwork, 1);
+    sidx = __shfl_sync(kFull, sidx, 0);
+    if (sidx >= hv_segs) break;
+    int lo = 0, hi = hv_count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(hv_segoff + mid) <= sidx) lo = mid; else hi = mid - 1;
+    }
+    const int32_t u = __ldg(hv_static + lo);
+    const u64 vis = visit[u];
+    if (vis == full) continue;
+    const int s0 = __ldg(hv_segoff + lo);
+    const int nseg = __ldg(hv_segoff + lo + 1) - s0;
+    const int rbeg = t_row_ptr[u], rend = t_row_ptr[u + 1];
+    const int ks = rbeg + (sidx - s0) * kPullSeg, ke = min(ks + kPullSeg, rend);
+    u64* hacc = hv_acc + 2 * (size_t)lo;
+    u64 w = 0;
+    for (int k0 = ks; k0 < ke; k0 += 128) {
+      const int k = k0 + lane;
+      const int32_t v0 = k < ke ? __ldg(t_col + k) : -1;
+      const int32_t v1 = k + 32 < ke ? __ldg(t_col + k + 32) : -1;
+      const int32_t v2 = k + 64 < ke ? __ldg(t_col + k + 64) : -1;
+      const int32_t v3 = k + 96 < ke ? __ldg(t_col + k + 96) : -1;
+      const u64 x0 = v0 >= 0 ? __ldg(fin + v0) : 0ull;
+      const u64 x1 = v1 >= 0 ? __ldg(fin + v1) : 0ull;
+      const u64 x2 = v2 >= 0 ? __ldg(fin + v2) : 0ull;
+      const u64 x3 = v3 >= 0 ? __ldg(fin + v3) : 0ull;
+      w |= x0 | x1 | x2 | x3;
+      if ((warp_or64(w) | vis | __ldcg(hacc)) == full) break;
+    }
+    w = warp_or64(w);
+    int last = 0;
+    if (lane == 0) {
+      if (w) atomicOr(hacc, w);
+      __threadfence();
+      last = atomicAdd(hacc + 1, 1ull) == (u64)(nseg - 1);
+    }
+    last = __shfl_sync(kFull, last, 0);
+    if (!last) continue;
+    u64 nw = 0;
+    int odeg = 0, ors = 0;
+    if (lane == 0) {
+      __threadfence();
+      const u64 got = atomicOr(hacc, 0ull);
+      hacc[0] = 0ull;
+      hacc[1] = 0ull;
+      nw = got & ~vis;
+      if (nw) {
+        visit[u] = vis | nw;
+        fout[u] = nw;
+        record_level(slices, n, u, nw, L);
+        ors = row_ptr[u];
+        odeg = row_ptr[u + 1] - ors;
+        acc.add((u64)odeg, (u64)(rend - rbeg), nw, (vis | nw) == full);
+      }
+    }
+    emit_routed(nw != 0ull, u, odeg, ors, aq_out, aq_count, seg_out, al_pack);
+  }
+  // Light rows: warps take 32 list entries at a time from a shared counter
+  // (row lengths differ widely; static striding does not balance them).
   for (;;) {
     int base = 0;
     if (lane == 0) base = atomicAdd(&ctl->work, 32);
@@ -457,6 +527,7 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphCondition
   ctl->mu_dec = 0;
   ctl->tq_size = 0;
   ctl->work = 0;
+  ctl->hwork = 0;
   const int nf = ctl->aq_size[L % 3] + long_vertices(ctl->alpack[L % 3]);
   if (nf == 0 || L >= n) {
     ctl->done = 1;
@@ -499,53 +570,71 @@ void probe_bs(const void* p, LevelProbe* out) {
   out->unvisited_edges = c->mu;
 }
 
-// Static pull list: every vertex with an in-edge, in descending order of
-// log2(in-degree) and by id within a class.  Heavy rows are taken first,
-// so the last chunks of a pull sweep are light ones and the sweep has no
-// long tail; lists filtered from it keep roughly the same order.
-__device__ __forceinline__ int degree_class(const int32_t* __restrict__ t_row_ptr, int32_t i) {
-  const int d = t_row_ptr[i + 1] - t_row_ptr[i];
-  return d > 0 ? 32 - __clz(d) : 0;  // 1..31, 0 = no in-edge
-}
-
-__global__ void flag_degree_class(const int32_t* __restrict__ t_row_ptr, int32_t n, int cls,
-                                  int64_t* __restrict__ flags) {
+// Static pull lists.  Light rows (0 < in-degree < kPullHeavy) are swept in
+// id order, 32 per warp task; heavy rows are cut into kPullSeg-entry
+// segments, one warp task each, so a hub row that cannot stop early is
+// spread over many warps instead of holding one warp for the whole level.
+__global__ void flag_rows(const int32_t* __restrict__ t_row_ptr, int32_t n, int heavy, int64_t* __restrict__ flags,
+                          int64_t* __restrict__ segs) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride)
-    flags[i] = degree_class(t_row_ptr, (int32_t)i) == cls ? 1 : 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride) {
+    const int d = t_row_ptr[i + 1] - t_row_ptr[i];
+    const bool h = d >= kPullHeavy;
+    flags[i] = heavy ? h : (d > 0 && !h);
+    if (segs) segs[i] = h ? (d + kPullSeg - 1) / kPullSeg : 0;
+  }
 }
 
 __global__ void scatter_flagged(const int64_t* __restrict__ flags, const int64_t* __restrict__ pos, int32_t n,
-                                int64_t base, int32_t* __restrict__ out) {
+                                int32_t* __restrict__ out, const int64_t* __restrict__ segpos,
+                                int32_t* __restrict__ segoff) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride)
-    if (flags[i]) out[base + pos[i]] = (int32_t)i;
+    if (flags[i]) {
+      out[pos[i]] = (int32_t)i;
+      if (segoff) segoff[pos[i]] = (int32_t)segpos[i];
+    }
 }
 
 dawn_status build_static_list(dawn_graph* g) {
   if (g->ul_static.p) return DAWN_OK;
   const int32_t n = g->n;
+  const size_t n1 = (size_t)n + 1;
   int64_t* tmp = nullptr;
-  DAWN_CUDA(cudaMallocAsync(&tmp, sizeof(int64_t) * 2 * ((size_t)n + 1), g->stream));
-  int64_t* flags = tmp;
-  int64_t* pos = tmp + n + 1;
+  DAWN_CUDA(cudaMallocAsync(&tmp, sizeof(int64_t) * 4 * n1, g->stream));
+  int64_t *flags = tmp, *pos = tmp + n1, *segs = tmp + 2 * n1, *segpos = tmp + 3 * n1;
+  int64_t cnt[2] = {0, 0}, nseg = 0;
   DAWN_CHECK(ensure(g->ul_static, sizeof(int32_t) * (size_t)n));
-  int64_t base = 0;
-  for (int cls = 31; cls >= 1; cls--) {
-    flag_degree_class<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->t_row_ptr, n, cls, flags);
+  DAWN_CHECK(ensure(g->hv_static, sizeof(int32_t) * (size_t)n));
+  DAWN_CHECK(ensure(g->hv_segoff, sizeof(int32_t) * n1));
+  for (int heavy = 0; heavy < 2; heavy++) {
+    flag_rows<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->t_row_ptr, n, heavy, flags, heavy ? segs : nullptr);
     DAWN_CUDA(cudaGetLastError());
     DAWN_CUDA(cudaMemsetAsync(flags + n, 0, sizeof(int64_t), g->stream));
-    DAWN_CHECK(exclusive_scan_i64(flags, pos, (int64_t)n + 1, g->stream));
-    scatter_flagged<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(flags, pos, n, base, g->ul_static.as<int32_t>());
+    DAWN_CHECK(exclusive_scan_i64(flags, pos, (int64_t)n1, g->stream));
+    if (heavy) {
+      DAWN_CUDA(cudaMemsetAsync(segs + n, 0, sizeof(int64_t), g->stream));
+      DAWN_CHECK(exclusive_scan_i64(segs, segpos, (int64_t)n1, g->stream));
+    }
+    scatter_flagged<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(
+        flags, pos, n, heavy ? g->hv_static.as<int32_t>() : g->ul_static.as<int32_t>(), heavy ? segpos : nullptr,
+        heavy ? g->hv_segoff.as<int32_t>() : nullptr);
     DAWN_CUDA(cudaGetLastError());
-    int64_t cnt = 0;
-    DAWN_CUDA(cudaMemcpyAsync(&cnt, pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, g->stream));
+    DAWN_CUDA(cudaMemcpyAsync(&cnt[heavy], pos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, g->stream));
+    if (heavy) DAWN_CUDA(cudaMemcpyAsync(&nseg, segpos + n, sizeof(int64_t), cudaMemcpyDeviceToHost, g->stream));
     DAWN_CUDA(cudaStreamSynchronize(g->stream));
-    base += cnt;
   }
+  // closing offset of the heavy segment prefix
+  const int32_t total = (int32_t)nseg;
+  DAWN_CUDA(cudaMemcpyAsync(g->hv_segoff.as<int32_t>() + cnt[1], &total, sizeof(int32_t), cudaMemcpyHostToDevice,
+                            g->stream));
+  DAWN_CHECK(ensure(g->hv_acc, 16 * (size_t)(cnt[1] > 0 ? cnt[1] : 1)));
+  DAWN_CUDA(cudaMemsetAsync(g->hv_acc.p, 0, 16 * (size_t)(cnt[1] > 0 ? cnt[1] : 1), g->stream));
   DAWN_CUDA(cudaFreeAsync(tmp, g->stream));
   DAWN_CUDA(cudaStreamSynchronize(g->stream));
-  g->ul_static_size = (int32_t)base;
+  g->ul_static_size = (int32_t)cnt[0];
+  g->hv_count = (int32_t)cnt[1];
+  g->hv_segs = (int32_t)nseg;
   return DAWN_OK;
 }
 
@@ -581,7 +670,9 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
     int32_t *aq, *aq0, *tq, *ul;
     Seg* segs;
     size_t segcap;
-    int32_t ul_static_size;
+    int32_t ul_static_size, hv_count, hv_segs;
+    const int32_t *hv_static, *hv_segoff;
+    u64* hv_acc;
     size_t nwords;
     int32_t n;
     long long m;
@@ -595,6 +686,11 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   a.t_col = g->t_col;
   a.ul_static = g->ul_static.as<int32_t>();
   a.ul_static_size = g->ul_static_size;
+  a.hv_static = g->hv_static.as<int32_t>();
+  a.hv_segoff = g->hv_segoff.as<int32_t>();
+  a.hv_acc = g->hv_acc.as<u64>();
+  a.hv_count = g->hv_count;
+  a.hv_segs = g->hv_segs;
   a.words = g->bs_words.as<u64>();
   a.visit = a.words;
   a.fr = a.words + nn;
@@ -615,7 +711,8 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   void* clear_args[] = {&a.words, &a.nwords};
   void* init_args[] = {&a.ctl, &a.row_ptr, &a.t_row_ptr, &a.visit, &a.fr0, &a.aq0, &a.segs, &a.n, &a.m};
   void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.slices, &a.aq, &a.segs,
-                       &a.segcap, &a.ul_static, &a.ul_static_size, &a.ul, &a.n};
+                       &a.segcap, &a.ul_static, &a.ul_static_size, &a.ul, &a.hv_static, &a.hv_segoff,
+                       &a.hv_acc, &a.hv_count, &a.hv_segs, &a.n};
   void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
                           &a.segcap, &a.tq, &a.n};
   void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,

@@ -126,3 +126,12 @@ def test_long_rows_span_tiles():
     g = hub_graph()
     check(g, np.array([0, 1, 1 + 1500 + 7], np.int32))
     check(g, np.arange(0, 200, dtype=np.int32), variants=[abi.VARIANT_BITSET])
+
+
+def test_heavy_pull_rows():
+    # hubs with in-degree in the tens of thousands: pull levels cut them into
+    # segments combined across warps
+    g = gen.rmat(17, 32, a=0.62, b=0.17, c=0.17, seed=14)
+    assert g.degrees().max() > 20000
+    srcs = gen.sources(g, 130, seed=15)
+    check(g, srcs, variants=[abi.VARIANT_BITSET])
