@@ -78,6 +78,7 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
@@ -97,6 +98,7 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
 
   unsigned long long my_mf = 0;
+  WarpQueue wq(s_q[wib], qout, qcount);
   auto op = [&](int32_t, int k, bool valid) {
     const int32_t u = valid ? __ldg(col + k) : -1;
     const bool found = valid && claim_bit(vbm, u);
@@ -108,10 +110,11 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
       atomicOr(fout + (u >> 5), 1u << (u & 31));
       my_mf += (unsigned long long)deg;
     }
-    emit_routed(found, u, deg, rs, qout, qcount, sout, lpack);
+    emit_routed(found, u, deg, rs, wq, sout, lpack);
   };
   seg_expand(row_ptr, sin, ln, op);
   warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
+  wq.flush();
   my_mf = warp_sum(my_mf);
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }
@@ -122,6 +125,7 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
                                                    int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
                                                    uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
                                                    int32_t n, int32_t nwords) {
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
   if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
   const int pout = L & 1;
@@ -139,6 +143,7 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
 
   unsigned long long my_mf = 0;
+  WarpQueue wq(s_q[threadIdx.x >> 5], qout, qcount);
   for (int w = global_warp(); w < nwords; w += num_warps()) {
     const uint32_t vis = vbm[w];
     uint32_t unv = ~vis;
@@ -168,9 +173,10 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
         dist[u] = L;
         my_mf += (unsigned long long)deg;
       }
-      emit_routed(found, u, deg, rs, qout, qcount, sout, lpack);
+      emit_routed(found, u, deg, rs, wq, sout, lpack);
     }
   }
+  wq.flush();
   my_mf = warp_sum(my_mf);
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }

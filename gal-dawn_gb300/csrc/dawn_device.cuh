@@ -192,3 +192,61 @@ __device__ __forceinline__ void seg_expand(const int32_t* __restrict__ row_ptr, 
 }
 
 }  // namespace dawn
+
+namespace dawn {
+
+// Per-warp staging of queue appends in shared memory.  Appending straight
+// to a global queue costs one atomicAdd on the queue's single counter per
+// warp step; with thousands of warps those same-address atomics serialise.
+// Here a warp collects up to kWarpQueue entries (warp-synchronously, no
+// atomics) and reserves global space once per full buffer.  All 32 lanes
+// must make every call; flush() must run before the warp exits.
+constexpr int kWarpQueue = 64;
+
+struct WarpQueue {
+  int32_t* buf;      // this warp's kWarpQueue shared-memory slots
+  int32_t* out;      // global queue
+  int32_t* count;    // global queue length
+  int n = 0;         // staged entries (warp-uniform)
+
+  __device__ __forceinline__ WarpQueue(int32_t* sbuf, int32_t* q, int32_t* cnt) : buf(sbuf), out(q), count(cnt) {}
+
+  __device__ __forceinline__ void flush() {
+    if (n == 0) return;
+    int base = 0;
+    if (lane_id() == 0) base = atomicAdd(count, n);
+    base = __shfl_sync(kFull, base, 0);
+    __syncwarp();
+    for (int i = lane_id(); i < n; i += 32) out[base + i] = buf[i];
+    __syncwarp();
+    n = 0;
+  }
+
+  __device__ __forceinline__ void push(bool pred, int32_t v) {
+    const uint32_t m = __ballot_sync(kFull, pred);
+    if (m == 0) return;
+    const int c = __popc(m);
+    if (n + c > kWarpQueue) flush();
+    if (pred) buf[n + __popc(m & lanemask_lt())] = v;
+    n += c;
+  }
+};
+
+// emit_routed with the short-row queue staged through a WarpQueue.
+__device__ __forceinline__ void emit_routed(bool found, int32_t u, int deg, int rs, WarpQueue& q_short,
+                                            Seg* __restrict__ segs, unsigned long long* lpack) {
+  const bool is_long = found && deg >= kLongRow;
+  q_short.push(found && !is_long, u);
+  const uint32_t lm = __ballot_sync(kFull, is_long);
+  if (lm) {
+    const int nseg = is_long ? (deg + kSeg - 1) / kSeg : 0;
+    const int incl = warp_incl_scan(nseg);
+    const int tot = __shfl_sync(kFull, incl, 31);
+    unsigned long long base = 0;
+    if (lane_id() == 0) base = atomicAdd(lpack, ((unsigned long long)__popc(lm) << 32) | (unsigned)tot);
+    const uint32_t b = (uint32_t)__shfl_sync(kFull, base, 0);
+    for (int j = 0; j < nseg; j++) segs[b + incl - nseg + j] = Seg{u, rs + j * kSeg};
+  }
+}
+
+}  // namespace dawn

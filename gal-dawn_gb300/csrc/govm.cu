@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
   if (ctl->done) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
@@ -117,6 +118,7 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
     atomicAnd(inq_in + (v >> 5), ~(1u << (v & 31)));
   }
 
+  WarpQueue wq(s_q[wib], qout, qcount);
   auto op = [&](int32_t v, int k, bool valid) {
     bool found = false;
     int32_t u = -1;
@@ -135,10 +137,11 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
       rs = row_ptr[u];
       deg = row_ptr[u + 1] - rs;
     }
-    emit_routed(found, u, deg, rs, qout, qcount, sout, lpack);
+    emit_routed(found, u, deg, rs, wq, sout, lpack);
   };
   seg_expand(row_ptr, sin, ln, op);
   warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
+  wq.flush();
 }
 
 __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop, int in_graph) {

@@ -203,6 +203,8 @@ __global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ u64 s_acc[kBlock / 32][32];
+  __shared__ int32_t s_qa[kBlock / 32][kWarpQueue];
+  __shared__ int32_t s_qu[kBlock / 32][kWarpQueue];
   if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
   const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n;
@@ -223,6 +225,8 @@ __global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__
   const u64 full = ctl->full;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   LevelAcc acc;
+  WarpQueue qa(s_qa[wib], aq_out, aq_count);
+  WarpQueue qu(s_qu[wib], ul_out, ul_count);
   // Heavy rows first, one kPullSeg-entry segment per warp task.  Each
   // segment ORs its gathers into the row's accumulator; the warp finishing
   // the row's last segment folds the accumulator into the vertex.  Only
@@ -286,7 +290,7 @@ __global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__
         acc.add((u64)odeg, (u64)(rend - rbeg), nw, (vis | nw) == full);
       }
     }
-    emit_routed(nw != 0ull, u, odeg, ors, aq_out, aq_count, seg_out, al_pack);
+    emit_routed(nw != 0ull, u, odeg, ors, qa, seg_out, al_pack);
   }
   // Light rows: warps take 32 list entries at a time from a shared counter
   // (row lengths differ widely; static striding does not balance them).
@@ -379,10 +383,11 @@ __global__ void __launch_bounds__(kBlock, 5) bs_pull(const int32_t* __restrict__
       odeg = row_ptr[u + 1] - ors;
       acc.add((u64)odeg, (u64)deg, nw, !still);
     }
-    const int pos = warp_append(still, ul_count);
-    if (still) ul_out[pos] = u;
-    emit_routed(nw != 0ull, u, odeg, ors, aq_out, aq_count, seg_out, al_pack);
+    qu.push(still, u);
+    emit_routed(nw != 0ull, u, odeg, ors, qa, seg_out, al_pack);
   }
+  qa.flush();
+  qu.flush();
   acc.flush(ctl, L % 3);
 }
 
@@ -401,6 +406,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n;
@@ -413,6 +419,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
                segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
   clear_next_slice(slices, n, L, ctl->nbits);
   const int wib = threadIdx.x >> 5;
+  WarpQueue wq(s_q[wib], tq, &ctl->tq_size);
   auto op = [&](int32_t v, int k, bool valid) {
     bool first = false;
     int32_t u = -1;
@@ -427,13 +434,11 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
           first = atomicOr(nxt + u, bits) == 0ull;
       }
     }
-    if (!dense) {
-      const int pos = warp_append(first, &ctl->tq_size);
-      if (first) tq[pos] = u;
-    }
+    if (!dense) wq.push(first, u);
   };
   seg_expand(row_ptr, seg_in, ln, op);
   warp_expand(row_ptr, aq_in, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
+  wq.flush();
 }
 
 // Push, phase 2: fold `next` into visited / frontier / level slices, over
@@ -445,6 +450,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
                                                          u64* __restrict__ slices, int32_t* __restrict__ aq,
                                                          Seg* __restrict__ segs, size_t segcap,
                                                          const int32_t* __restrict__ tq, int32_t n) {
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   u64* __restrict__ fout = fr + (size_t)(L % 3) * n;
@@ -452,6 +458,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
   Seg* seg_out = segs + (size_t)(L % 3) * segcap;
   const u64 full = ctl->full;
   const bool dense = ctl->dense != 0;
+  WarpQueue wq(s_q[threadIdx.x >> 5], aq_out, &ctl->aq_size[L % 3]);
   const int tn = dense ? n : ctl->tq_size;
   LevelAcc acc;
   const int total = gridDim.x * blockDim.x;
@@ -477,13 +484,33 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
         }
       }
     }
-    emit_routed(nw != 0ull, u, odeg, ors, aq_out, &ctl->aq_size[L % 3], seg_out, &ctl->alpack[L % 3]);
+    emit_routed(nw != 0ull, u, odeg, ors, wq, seg_out, &ctl->alpack[L % 3]);
   }
+  wq.flush();
   acc.flush(ctl, L % 3);
 }
 
 // Expands the level slices of one batch into its distance rows: thread per
 // vertex, one store per source, consecutive vertices per warp (full lines).
+// NB is the number of level bits in use (template for the common <= 8).
+template <int NB>
+__device__ __forceinline__ void emit_vertex(int32_t* __restrict__ dist, int32_t n, int nb_src, size_t u, u64 vis,
+                                            const u64* __restrict__ slices, int nbits) {
+  u64 w[NB > 0 ? NB : 1];
+#pragma unroll
+  for (int k = 0; k < NB; k++) w[k] = slices[(size_t)k * n + u];
+  for (int s = 0; s < nb_src; s++) {
+    int32_t v = -1;
+    if ((vis >> s) & 1ull) {
+      v = 0;
+#pragma unroll
+      for (int k = 0; k < NB; k++) v |= (int32_t)((w[k] >> s) & 1ull) << k;
+      for (int k = NB; k < nbits; k++) v |= (int32_t)((slices[(size_t)k * n + u] >> s) & 1ull) << k;
+    }
+    dist[(size_t)s * n + u] = v;
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__ ctl, const u64* __restrict__ visit,
                                                        const u64* __restrict__ slices, int32_t n) {
   const int batch = ctl->batch;
@@ -493,18 +520,15 @@ __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < (size_t)n; u += stride) {
     const u64 vis = visit[u];
-    u64 w[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) w[k] = k < nbits ? slices[(size_t)k * n + u] : 0ull;
-    for (int s = 0; s < nb; s++) {
-      int32_t v = -1;
-      if ((vis >> s) & 1ull) {
-        v = 0;
-#pragma unroll
-        for (int k = 0; k < 8; k++) v |= (int32_t)((w[k] >> s) & 1ull) << k;
-        for (int k = 8; k < nbits; k++) v |= (int32_t)((slices[(size_t)k * n + u] >> s) & 1ull) << k;
-      }
-      dist[(size_t)s * n + u] = v;
+    switch (nbits) {
+      case 1: emit_vertex<1>(dist, n, nb, u, vis, slices, nbits); break;
+      case 2: emit_vertex<2>(dist, n, nb, u, vis, slices, nbits); break;
+      case 3: emit_vertex<3>(dist, n, nb, u, vis, slices, nbits); break;
+      case 4: emit_vertex<4>(dist, n, nb, u, vis, slices, nbits); break;
+      case 5: emit_vertex<5>(dist, n, nb, u, vis, slices, nbits); break;
+      case 6: emit_vertex<6>(dist, n, nb, u, vis, slices, nbits); break;
+      case 7: emit_vertex<7>(dist, n, nb, u, vis, slices, nbits); break;
+      default: emit_vertex<8>(dist, n, nb, u, vis, slices, nbits); break;
     }
   }
 }
