@@ -367,23 +367,34 @@ def main():
     col_h = torch.from_numpy(g.col).pin_memory()
     out_h = torch.empty((NSRC, g.n), dtype=torch.int32).pin_memory()
 
-    def e2e_step():
+    phases = {"create_ms": 0.0, "bfs_ms": 0.0, "destroy_ms": 0.0}
+
+    def e2e_step(record=False):
+        t0 = time.perf_counter()
         h = abi.Graph(raw=dict(n=g.n, m=g.m, row_ptr=rp_h.data_ptr(), col=col_h.data_ptr(), symmetric=True,
                                stream=stream))
+        t1 = time.perf_counter()
         h.bfs_host_ptr(srcs, out_h.data_ptr(), variant=abi.VARIANT_BITSET)
+        t2 = time.perf_counter()
         h.close()
+        t3 = time.perf_counter()
+        if record:
+            phases["create_ms"] += (t1 - t0) * 1e3
+            phases["bfs_ms"] += (t2 - t1) * 1e3
+            phases["destroy_ms"] += (t3 - t2) * 1e3
 
     e2e_step()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        e2e_step()
+        e2e_step(record=True)
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
     h2d = 4 * (g.n + 1) + 4 * g.m + 4 * NSRC
     d2h = 4 * NSRC * g.n
     e2e = {"value": round(edges / (e2e_ms * 1e-3) / 1e9 * ws, 3), "unit": "GTEPS", "ms_per_step": round(e2e_ms, 3),
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "phases_ms": {k: round(v / args.e2e_steps, 3) for k, v in phases.items()},
            "call": "dawn_graph_create(pinned host CSR) + dawn_bfs(pinned host dist) + dawn_graph_destroy"}
 
     cpu = None

@@ -71,24 +71,27 @@ dawn_status start_graph(dawn_wtype wtype, int32_t n, int64_t m, uint32_t flags, 
     DAWN_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
     g->own_stream = true;
   }
-  DAWN_CUDA(cudaMalloc(&g->row_ptr, sizeof(int32_t) * ((size_t)n + 1)));
-  DAWN_CUDA(cudaMalloc(&g->col, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
-  if (wtype != DAWN_W_NONE) DAWN_CUDA(cudaMalloc(&g->val, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
+  // col / val carry 16 spare bytes so 128-bit loads at a row's end stay in bounds.
+  DAWN_CHECK(dawn::pool_alloc((void**)&g->row_ptr, sizeof(int32_t) * ((size_t)n + 1), g->stream));
+  DAWN_CHECK(dawn::pool_alloc((void**)&g->col, sizeof(int32_t) * (size_t)(m > 0 ? m : 1) + 16, g->stream));
+  if (wtype != DAWN_W_NONE)
+    DAWN_CHECK(dawn::pool_alloc(&g->val, sizeof(int32_t) * (size_t)(m > 0 ? m : 1) + 16, g->stream));
   return DAWN_OK;
 }
 
 void destroy(dawn_graph* g) {
   if (!g) return;
   if (g->stream) cudaStreamSynchronize(g->stream);
-  if (g->t_row_ptr && g->t_row_ptr != g->row_ptr) cudaFree(g->t_row_ptr);
-  if (g->t_col && g->t_col != g->col) cudaFree(g->t_col);
-  cudaFree(g->row_ptr);
-  cudaFree(g->col);
-  if (g->val) cudaFree(g->val);
+  if (g->t_row_ptr && g->t_row_ptr != g->row_ptr) dawn::pool_free(g->t_row_ptr, g->stream);
+  if (g->t_col && g->t_col != g->col) dawn::pool_free(g->t_col, g->stream);
+  dawn::pool_free(g->row_ptr, g->stream);
+  dawn::pool_free(g->col, g->stream);
+  if (g->val) dawn::pool_free(g->val, g->stream);
   DevBuf* bufs[] = {&g->ss_queues, &g->ss_segs, &g->bs_segs, &g->ss_bitmaps, &g->ss_ctl, &g->ss_sources, &g->ss_scratch,
                     &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
                     &g->dist_stage};
   for (DevBuf* b : bufs) dawn::release(*b);
+  if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
   if (g->sssp_exec) cudaGraphExecDestroy(g->sssp_exec);
   if (g->bs_exec) cudaGraphExecDestroy(g->bs_exec);
@@ -158,7 +161,7 @@ dawn_status sssp_device_impl(dawn_graph* g, const int32_t* sources, int32_t nsrc
     st->batches = nsrc;
     DAWN_CUDA(cudaEventElapsedTime(&st->device_ms, g->ev0, g->ev1));
     // TEPS numerator: out-degree sum of the reached vertices of every row.
-    DAWN_CHECK(dawn::ensure(g->cc_out, 16 * (size_t)nsrc));
+    DAWN_CHECK(dawn::ensure(g->cc_out, 16 * (size_t)nsrc, g->stream));
     double* sum = g->cc_out.as<double>();
     long long* cnt = reinterpret_cast<long long*>(sum + nsrc);
     DAWN_CHECK(dawn::row_reduce(g, d_dist, nsrc, g->ss_sources.as<int32_t>(), g->wtype == DAWN_W_F32 ? 2 : 1,
@@ -182,15 +185,33 @@ void add_stats(dawn_stats* acc, const dawn_stats& s) {
 
 // Runs a device traversal in chunks of sources through device staging and
 // copies each chunk's rows to the caller's host array.
+bool is_pinned_host(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 template <class Fn>
 dawn_status staged(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* host_dist, size_t elem,
-                   dawn_stats* st, Fn&& run) {
+                   dawn_stats* st, Fn&& run, bool direct_ok = false) {
   const size_t row_bytes = elem * (size_t)g->n;
+  if (direct_ok && is_pinned_host(host_dist)) {
+    // The traversal writes its distances only in its final pass, so the
+    // caller's page-locked buffer can take them directly over the host
+    // link: no device staging and no separate copy.
+    DAWN_CHECK(run(sources, nsrc, host_dist, st));
+    DAWN_CUDA(cudaStreamSynchronize(g->stream));
+    return DAWN_OK;
+  }
   int32_t chunk = (int32_t)(kStageBytes / row_bytes);
   if (chunk >= 64) chunk -= chunk % 64;
   if (chunk < 1) chunk = 1;
   if (chunk > nsrc) chunk = nsrc;
-  DAWN_CHECK(dawn::ensure(g->dist_stage, row_bytes * (size_t)chunk));
+  DAWN_CHECK(dawn::ensure(g->dist_stage, row_bytes * (size_t)chunk, g->stream));
   if (st) std::memset(st, 0, sizeof(*st));
   for (int32_t i0 = 0; i0 < nsrc; i0 += chunk) {
     const int32_t c = nsrc - i0 < chunk ? nsrc - i0 : chunk;
@@ -333,10 +354,13 @@ dawn_status dawn_bfs(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return DAWN_OK;
   }
-  return staged(g, sources, nsrc, dist, sizeof(int32_t), stats,
-                [&](const int32_t* s, int32_t c, void* d, dawn_stats* st) {
-                  return bfs_device_impl(g, s, c, static_cast<int32_t*>(d), variant, st);
-                });
+  const int32_t v = resolve_variant(variant, nsrc);
+  return staged(
+      g, sources, nsrc, dist, sizeof(int32_t), stats,
+      [&](const int32_t* s, int32_t c, void* d, dawn_stats* st) {
+        return bfs_device_impl(g, s, c, static_cast<int32_t*>(d), variant, st);
+      },
+      v == DAWN_VARIANT_BITSET || v == DAWN_VARIANT_LEARNED);
 }
 
 dawn_status dawn_sssp_device(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist, int32_t variant,
@@ -402,10 +426,10 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, 
   if (chunk >= 64) chunk -= chunk % 64;
   if (chunk < 1) chunk = 1;
   if (chunk > nsrc) chunk = nsrc;
-  DAWN_CHECK(dawn::ensure(g->dist_stage, row_bytes * (size_t)chunk));
-  DAWN_CHECK(dawn::ensure(g->cc_out, 16 * (size_t)chunk));
+  DAWN_CHECK(dawn::ensure(g->dist_stage, row_bytes * (size_t)chunk, g->stream));
+  DAWN_CHECK(dawn::ensure(g->cc_out, 16 * (size_t)chunk, g->stream));
   DevBuf srcbuf;
-  DAWN_CHECK(dawn::ensure(srcbuf, sizeof(int32_t) * (size_t)chunk));
+  DAWN_CHECK(dawn::ensure(srcbuf, sizeof(int32_t) * (size_t)chunk, g->stream));
   std::vector<double> hsum(chunk);
   std::vector<long long> hcnt(chunk);
   dawn_status s = DAWN_OK;

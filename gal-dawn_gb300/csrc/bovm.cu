@@ -242,12 +242,12 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   const int32_t n = g->n;
   int32_t nwords = (n + 31) / 32;
   long long m = g->m;
-  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * (size_t)n));
+  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * (size_t)n, g->stream));
   size_t segcap = seg_capacity(n, m);
-  DAWN_CHECK(ensure(g->ss_segs, sizeof(Seg) * 2 * segcap));
-  DAWN_CHECK(ensure(g->ss_bitmaps, sizeof(uint32_t) * 4 * (size_t)nwords));
-  DAWN_CHECK(ensure(g->ss_ctl, sizeof(SsCtl)));
-  DAWN_CHECK(ensure(g->ss_sources, sizeof(int32_t) * (size_t)nsrc));
+  DAWN_CHECK(ensure(g->ss_segs, sizeof(Seg) * 2 * segcap, g->stream));
+  DAWN_CHECK(ensure(g->ss_bitmaps, sizeof(uint32_t) * 4 * (size_t)nwords, g->stream));
+  DAWN_CHECK(ensure(g->ss_ctl, sizeof(SsCtl), g->stream));
+  DAWN_CHECK(ensure(g->ss_sources, sizeof(int32_t) * (size_t)nsrc, g->stream));
   DAWN_CUDA(cudaMemcpyAsync(g->ss_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
                             g->stream));
   SsCtl c = {};

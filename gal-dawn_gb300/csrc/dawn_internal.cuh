@@ -35,16 +35,22 @@ constexpr uint32_t kFull = 0xffffffffu;
 constexpr int kBlock = 256;  // threads per CTA of the frontier kernels
 
 // Device buffer owned by a graph handle; grows on demand, never shrinks.
+// Storage comes from the device's stream-ordered memory pool, which keeps
+// freed blocks, so creating and destroying handles repeatedly does not go
+// back to the driver each time.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;
   template <class T>
   T* as() const {
     return static_cast<T*>(p);
   }
 };
-dawn_status ensure(DevBuf& b, size_t bytes);
+dawn_status ensure(DevBuf& b, size_t bytes, cudaStream_t s);
 void release(DevBuf& b);
+dawn_status pool_alloc(void** p, size_t bytes, cudaStream_t s);
+void pool_free(void* p, cudaStream_t s);
 
 // --- single-source frontier traversal (BOVM push/pull, GOVM push) ---------
 

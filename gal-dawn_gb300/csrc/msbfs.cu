@@ -628,9 +628,9 @@ dawn_status build_static_list(dawn_graph* g) {
   DAWN_CUDA(cudaMallocAsync(&tmp, sizeof(int64_t) * 4 * n1, g->stream));
   int64_t *flags = tmp, *pos = tmp + n1, *segs = tmp + 2 * n1, *segpos = tmp + 3 * n1;
   int64_t cnt[2] = {0, 0}, nseg = 0;
-  DAWN_CHECK(ensure(g->ul_static, sizeof(int32_t) * (size_t)n));
-  DAWN_CHECK(ensure(g->hv_static, sizeof(int32_t) * (size_t)n));
-  DAWN_CHECK(ensure(g->hv_segoff, sizeof(int32_t) * n1));
+  DAWN_CHECK(ensure(g->ul_static, sizeof(int32_t) * (size_t)n, g->stream));
+  DAWN_CHECK(ensure(g->hv_static, sizeof(int32_t) * (size_t)n, g->stream));
+  DAWN_CHECK(ensure(g->hv_segoff, sizeof(int32_t) * n1, g->stream));
   for (int heavy = 0; heavy < 2; heavy++) {
     flag_rows<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->t_row_ptr, n, heavy, flags, heavy ? segs : nullptr);
     DAWN_CUDA(cudaGetLastError());
@@ -652,7 +652,7 @@ dawn_status build_static_list(dawn_graph* g) {
   const int32_t total = (int32_t)nseg;
   DAWN_CUDA(cudaMemcpyAsync(g->hv_segoff.as<int32_t>() + cnt[1], &total, sizeof(int32_t), cudaMemcpyHostToDevice,
                             g->stream));
-  DAWN_CHECK(ensure(g->hv_acc, 16 * (size_t)(cnt[1] > 0 ? cnt[1] : 1)));
+  DAWN_CHECK(ensure(g->hv_acc, 16 * (size_t)(cnt[1] > 0 ? cnt[1] : 1), g->stream));
   DAWN_CUDA(cudaMemsetAsync(g->hv_acc.p, 0, 16 * (size_t)(cnt[1] > 0 ? cnt[1] : 1), g->stream));
   DAWN_CUDA(cudaFreeAsync(tmp, g->stream));
   DAWN_CUDA(cudaStreamSynchronize(g->stream));
@@ -670,12 +670,12 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   DAWN_CHECK(build_static_list(g));
   // words: visit | fr[3] | nxt | level slices[nbits] ; lists: aq[3] | tq | ul[2] ; segments[3]
   const int nbits = 32 - __builtin_clz((unsigned)n);  // levels never exceed n
-  DAWN_CHECK(ensure(g->bs_words, sizeof(u64) * (5 + (size_t)nbits) * nn));
-  DAWN_CHECK(ensure(g->bs_queues, sizeof(int32_t) * 6 * nn));
+  DAWN_CHECK(ensure(g->bs_words, sizeof(u64) * (5 + (size_t)nbits) * nn, g->stream));
+  DAWN_CHECK(ensure(g->bs_queues, sizeof(int32_t) * 6 * nn, g->stream));
   const size_t segcap = seg_capacity(n, g->m);
-  DAWN_CHECK(ensure(g->bs_segs, sizeof(Seg) * 3 * segcap));
-  DAWN_CHECK(ensure(g->bs_ctl, sizeof(BsCtl)));
-  DAWN_CHECK(ensure(g->bs_sources, sizeof(int32_t) * (size_t)nsrc));
+  DAWN_CHECK(ensure(g->bs_segs, sizeof(Seg) * 3 * segcap, g->stream));
+  DAWN_CHECK(ensure(g->bs_ctl, sizeof(BsCtl), g->stream));
+  DAWN_CHECK(ensure(g->bs_sources, sizeof(int32_t) * (size_t)nsrc, g->stream));
   DAWN_CUDA(cudaMemcpyAsync(g->bs_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
                             g->stream));
   BsCtl c = {};

@@ -22,19 +22,42 @@ void set_error(const char* fmt, ...) {
 void clear_error() { g_err[0] = 0; }
 const char* last_error() { return g_err; }
 
-dawn_status ensure(DevBuf& b, size_t bytes) {
+namespace {
+std::once_flag g_pool_once[64];
+}
+
+dawn_status pool_alloc(void** p, size_t bytes, cudaStream_t s) {
+  int dev = 0;
+  DAWN_CUDA(cudaGetDevice(&dev));
+  std::call_once(g_pool_once[dev & 63], [dev]() {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  });
+  DAWN_CUDA(cudaMallocAsync(p, bytes ? bytes : 16, s));
+  return DAWN_OK;
+}
+
+void pool_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+dawn_status ensure(DevBuf& b, size_t bytes, cudaStream_t s) {
   if (bytes == 0) bytes = 16;
   if (b.bytes >= bytes) return DAWN_OK;
-  if (b.p) cudaFree(b.p);
+  if (b.p) pool_free(b.p, b.stream);
   b.p = nullptr;
   b.bytes = 0;
-  DAWN_CUDA(cudaMalloc(&b.p, bytes));
+  DAWN_CHECK(pool_alloc(&b.p, bytes, s));
   b.bytes = bytes;
+  b.stream = s;
   return DAWN_OK;
 }
 
 void release(DevBuf& b) {
-  if (b.p) cudaFree(b.p);
+  if (b.p) pool_free(b.p, b.stream);
   b.p = nullptr;
   b.bytes = 0;
 }
@@ -243,6 +266,19 @@ dawn_status ss_run(dawn_graph* g, SsFamily& fam, int32_t nruns, cudaGraphExec_t*
 
 namespace {
 
+__device__ __forceinline__ int check_entry(int32_t c, int32_t n, const void* val, int wtype, size_t k) {
+  int f = (c < 0 || c >= n) ? 8 : 0;
+  if (wtype == DAWN_W_I32 && static_cast<const int32_t*>(val)[k] < 0) f |= 16;
+  if (wtype == DAWN_W_F32) {
+    const float w = static_cast<const float*>(val)[k];
+    if (!(w >= 0.0f) || isinf(w)) f |= 16;
+  }
+  return f;
+}
+
+// One pass over row_ptr and col (128-bit loads) checking the CSR invariants
+// the kernels rely on: monotone row_ptr from 0 to m, columns in [0, n),
+// weights finite and non-negative.
 __global__ void validate_csr_kernel(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
                                     const void* __restrict__ val, int wtype, int32_t n, long long m,
                                     int* __restrict__ flags) {
@@ -255,15 +291,15 @@ __global__ void validate_csr_kernel(const int32_t* __restrict__ rp, const int32_
   }
   for (size_t i = tid; i < (size_t)n; i += stride)
     if (rp[i] > rp[i + 1]) f |= 4;
-  for (size_t k = tid; k < (size_t)m; k += stride) {
-    const int32_t c = col[k];
-    if (c < 0 || c >= n) f |= 8;
-    if (wtype == DAWN_W_I32 && static_cast<const int32_t*>(val)[k] < 0) f |= 16;
-    if (wtype == DAWN_W_F32) {
-      const float w = static_cast<const float*>(val)[k];
-      if (!(w >= 0.0f) || isinf(w)) f |= 16;
-    }
+  const size_t m4 = (size_t)m / 4;
+  const int4* c4 = reinterpret_cast<const int4*>(col);
+  for (size_t q = tid; q < m4; q += stride) {
+    const int4 c = c4[q];
+    const int32_t cc[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int j = 0; j < 4; j++) f |= check_entry(cc[j], n, val, wtype, 4 * q + j);
   }
+  for (size_t k = 4 * m4 + tid; k < (size_t)m; k += stride) f |= check_entry(col[k], n, val, wtype, k);
   if (f) atomicOr(flags, f);
 }
 
@@ -273,7 +309,7 @@ dawn_status validate_csr(dawn_graph* g) {
   int* d_flags = nullptr;
   DAWN_CUDA(cudaMallocAsync(&d_flags, sizeof(int), g->stream));
   DAWN_CUDA(cudaMemsetAsync(d_flags, 0, sizeof(int), g->stream));
-  validate_csr_kernel<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->row_ptr, g->col, g->val, g->wtype, g->n, g->m,
+  validate_csr_kernel<<<g->geo.sms * 8, kBlock, 0, g->stream>>>(g->row_ptr, g->col, g->val, g->wtype, g->n, g->m,
                                                                  d_flags);
   DAWN_CUDA(cudaGetLastError());
   int flags = 0;
@@ -395,8 +431,8 @@ dawn_status build_transpose(dawn_graph* g) {
   count_in_degree<<<grid, kBlock, 0, s>>>(g->col, g->m, deg);
   DAWN_CUDA(cudaGetLastError());
   DAWN_CHECK(exclusive_scan_i64(reinterpret_cast<const int64_t*>(deg), off, (int64_t)n + 1, s));
-  DAWN_CUDA(cudaMalloc(&g->t_row_ptr, sizeof(int32_t) * ((size_t)n + 1)));
-  DAWN_CUDA(cudaMalloc(&g->t_col, sizeof(int32_t) * (size_t)(g->m > 0 ? g->m : 1)));
+  DAWN_CHECK(pool_alloc((void**)&g->t_row_ptr, sizeof(int32_t) * ((size_t)n + 1), s));
+  DAWN_CHECK(pool_alloc((void**)&g->t_col, sizeof(int32_t) * (size_t)(g->m > 0 ? g->m : 1) + 16, s));
   offsets_to_rowptr<<<grid, kBlock, 0, s>>>(off, g->t_row_ptr, deg, n);
   DAWN_CUDA(cudaGetLastError());
   scatter_in_edges<<<grid, kBlock, 0, s>>>(g->row_ptr, g->col, n, deg, g->t_col);
