@@ -273,6 +273,65 @@ def run_reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def suite_lines(torch, abi, gen, stream, rank):
+    """The other workload shapes, one JSON line each (not the headline line):
+    directed ER n=65,536 x 64 sources (the CPU-runnable case), weighted
+    SSSP on the RMAT-22 topology x 64 sources (int32 and float32 weights),
+    and RMAT-18 x 4,096 sources."""
+    out = []
+
+    def timed(fn, steps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    # ER-64K directed, 64 sources
+    g = gen.erdos_renyi(65536, 1 << 20, seed=1)
+    srcs = gen.sources(g, 64, seed=2, from_lcc=False)
+    with abi.Graph(g, stream=stream) as dg:
+        d = torch.empty((64, g.n), dtype=torch.int32, device="cuda")
+        st = dg.bfs_device(srcs, d.data_ptr(), variant=abi.VARIANT_BITSET)
+        for var, name in ((abi.VARIANT_BITSET, "bitset"), (abi.VARIANT_DO, "plain")):
+            ms = timed(lambda: dg.bfs_device(srcs, d.data_ptr(), variant=var, stats=False), 10)
+            out.append({"suite": "er64k-directed-bfs-64src", "variant": name, "ms_per_step": round(ms, 4),
+                        "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2), "n": g.n, "m": g.m})
+    # weighted SSSP, RMAT-22 topology, 64 sources
+    g = gen.rmat(22, EDGEFACTOR, A, B, C, seed=GRAPH_SEED, weights=True)
+    srcs = gen.sources(g, NSRC, seed=SOURCE_SEED)
+    for w in ("i32", "f32"):
+        with abi.Graph(g, weights=w, stream=stream) as dg:
+            d = torch.empty((NSRC, g.n), dtype=torch.int32, device="cuda")
+            st = dg.sssp_device(srcs, d.data_ptr())
+            ms = timed(lambda: dg.sssp_device(srcs, d.data_ptr(), stats=False), 2)
+            out.append({"suite": "rmat22-sssp-64src", "weights": w, "ms_per_step": round(ms, 3),
+                        "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2),
+                        "levels_per_source": round(st.levels / NSRC, 1)})
+    del g
+    # RMAT-18, 4096 sources
+    g = gen.rmat(18, EDGEFACTOR, A, B, C, seed=GRAPH_SEED)
+    srcs = gen.sources(g, 4096, seed=SOURCE_SEED)
+    with abi.Graph(g, stream=stream) as dg:
+        d = torch.empty((4096, g.n), dtype=torch.int32, device="cuda")
+        st = dg.bfs_device(srcs, d.data_ptr(), variant=abi.VARIANT_BITSET)
+        ms = timed(lambda: dg.bfs_device(srcs, d.data_ptr(), variant=abi.VARIANT_BITSET, stats=False), 2)
+        out.append({"suite": "rmat18-bfs-4096src", "variant": "bitset", "ms_per_step": round(ms, 3),
+                    "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2), "n": g.n, "m": g.m})
+        ms = timed(lambda: dg.bfs_device(srcs[:256], d.data_ptr(), variant=abi.VARIANT_DO, stats=False), 1)
+        st2 = dg.bfs_device(srcs[:256], d.data_ptr(), variant=abi.VARIANT_DO)
+        out.append({"suite": "rmat18-bfs-4096src", "variant": "plain (first 256 sources)",
+                    "ms_per_step": round(ms, 3), "gteps": round(st2.edges_traversed / (ms * 1e-3) / 1e9, 2)})
+    if rank == 0:
+        for line in out:
+            print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -288,6 +347,8 @@ def main():
     ap.add_argument("--traced", action="store_true",
                     help="with --quick: run the steps level by level, launching only the kernels each level uses")
     ap.add_argument("--variant", default="bitset", choices=["bitset", "do", "push"])
+    ap.add_argument("--suite", action="store_true",
+                    help="also time the other workload shapes (one JSON line each, before the main line)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -301,6 +362,11 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
         barrier = dist.barrier
+    if args.suite:
+        from dawn_gb300 import gen as _gen
+        _s = torch.cuda.Stream()
+        torch.cuda.set_stream(_s)
+        suite_lines(torch, abi, _gen, _s.cuda_stream, rank)
     g, srcs = make_workload(args.scale, rank)
     # A dedicated stream: the library launches on it and torch's events
     # record on it (the legacy default stream has handle 0, which the C ABI
