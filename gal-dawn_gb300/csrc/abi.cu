@@ -94,7 +94,8 @@ void destroy(dawn_graph* g) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
   if (g->sssp_exec) cudaGraphExecDestroy(g->sssp_exec);
-  if (g->bs_exec) cudaGraphExecDestroy(g->bs_exec);
+  for (cudaGraphExec_t e : g->bs_exec)
+    if (e) cudaGraphExecDestroy(e);
   if (g->h_ctl) cudaFreeHost(g->h_ctl);
   for (cudaEvent_t e : g->trace_ev)
     if (e) cudaEventDestroy(e);
@@ -477,6 +478,52 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, 
   }
   dawn::release(srcbuf);
   return s;
+}
+
+dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value) {
+  dawn::clear_error();
+  if (!g) {
+    dawn::set_error("graph is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  switch (option) {
+    case DAWN_OPT_BITSET_WIDTH:
+      if (value != 0 && value != 1 && value != 2 && value != 4) {
+        dawn::set_error("bitset width must be 0 (automatic), 1, 2 or 4");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      g->bs_width = (int32_t)value;
+      return DAWN_OK;
+    case DAWN_OPT_PUSH_RATIO:
+      if (value < 1 || value > 1 << 20) {
+        dawn::set_error("push ratio must lie in [1, 2^20]");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      g->bs_push_ratio = (int32_t)value;
+      return DAWN_OK;
+    default:
+      dawn::set_error("unknown option %d", option);
+      return DAWN_ERR_INVALID_ARG;
+  }
+}
+
+dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option, int64_t* value) {
+  dawn::clear_error();
+  if (!g || !value) {
+    dawn::set_error("graph or value is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  switch (option) {
+    case DAWN_OPT_BITSET_WIDTH:
+      *value = g->bs_width;
+      return DAWN_OK;
+    case DAWN_OPT_PUSH_RATIO:
+      *value = g->bs_push_ratio;
+      return DAWN_OK;
+    default:
+      dawn::set_error("unknown option %d", option);
+      return DAWN_ERR_INVALID_ARG;
+  }
 }
 
 dawn_status dawn_trace_enable(dawn_graph* g, int32_t enable) {

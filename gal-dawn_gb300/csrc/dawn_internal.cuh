@@ -171,6 +171,7 @@ struct dawn_graph {
   dawn::DevBuf hv_acc;          // per heavy row: OR accumulator + finished-segment count
   int32_t hv_count = 0, hv_segs = 0;
   int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges
+  int32_t bs_width = 0;         // words per vertex of the bitset traversal (0 = by source count)
 
   // closeness reduction
   dawn::DevBuf cc_out;
@@ -182,7 +183,7 @@ struct dawn_graph {
   cudaGraphExec_t bfs_exec = nullptr;
   cudaGraphExec_t sssp_exec = nullptr;
   int32_t sssp_exec_weighted = -1;
-  cudaGraphExec_t bs_exec = nullptr;
+  cudaGraphExec_t bs_exec[3] = {nullptr, nullptr, nullptr};  // bitset width 1, 2, 4
 
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 
@@ -201,6 +202,7 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,
 dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                        int32_t* d_dist);
 dawn_status bfs_bitset_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc);
+int bitset_width(const dawn_graph* g, int32_t nsrc);
 // govm.cu
 dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                         void* d_dist);

@@ -23,8 +23,9 @@ LIB_PATH = os.path.join(LIB_DIR, "libdawn_gb300.so")
 # Every symbol the header declares; tests check the library exports them.
 EXPORTS = ("dawn_graph_create", "dawn_graph_create_device", "dawn_graph_destroy",
            "dawn_graph_set_stream", "dawn_graph_synchronize", "dawn_bfs", "dawn_bfs_device",
-           "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_trace_enable", "dawn_trace_read",
-           "dawn_last_error", "dawn_version")
+           "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_graph_set_option",
+           "dawn_graph_get_option", "dawn_trace_enable", "dawn_trace_read", "dawn_last_error", "dawn_version")
+OPT_BITSET_WIDTH, OPT_PUSH_RATIO = 1, 2
 
 
 class DawnError(RuntimeError):
@@ -75,6 +76,8 @@ def lib():
         L.dawn_sssp_device.argtypes = L.dawn_bfs.argtypes
         L.dawn_closeness.argtypes = [_VP, _VP, ctypes.c_int32, ctypes.c_int32, _VP, _VP, _VP,
                                      ctypes.POINTER(Stats)]
+        L.dawn_graph_set_option.argtypes = [_VP, ctypes.c_int32, ctypes.c_int64]
+        L.dawn_graph_get_option.argtypes = [_VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
         L.dawn_trace_enable.argtypes = [_VP, ctypes.c_int32]
         L.dawn_trace_read.argtypes = [_VP, ctypes.POINTER(TraceRec), ctypes.c_int64,
                                       ctypes.POINTER(ctypes.c_int64)]
@@ -172,6 +175,14 @@ class Graph:
 
     def synchronize(self):
         _check(lib().dawn_graph_synchronize(self.handle))
+
+    def set_option(self, option, value):
+        _check(lib().dawn_graph_set_option(self.handle, option, int(value)))
+
+    def get_option(self, option):
+        v = ctypes.c_int64()
+        _check(lib().dawn_graph_get_option(self.handle, option, ctypes.byref(v)))
+        return v.value
 
     def trace(self, enable=True):
         _check(lib().dawn_trace_enable(self.handle, int(enable)))

@@ -137,6 +137,21 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources,
                            double* dist_sum, int64_t* reached,
                            dawn_stats* stats);
 
+/* Tuning knobs of a handle (no counterpart in the reference, whose only
+ * knobs are the block size and stream count hard-coded in its tools,
+ * algorithm/gpu/mssp_gpu/mssp_gpu.cu:16-17).  The autotuner sets these;
+ * results never depend on them.
+ *   DAWN_OPT_BITSET_WIDTH  uint64 words per vertex of the batched traversal:
+ *                          0 = chosen from the source count, or 1, 2, 4
+ *                          (64, 128, 256 sources per batch)
+ *   DAWN_OPT_PUSH_RATIO    a level pushes while ratio x frontier edges <
+ *                          edges of unfinished vertices (default 4) */
+#define DAWN_OPT_BITSET_WIDTH 1
+#define DAWN_OPT_PUSH_RATIO 2
+dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value);
+dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option,
+                                  int64_t* value);
+
 /* Per-level trace.  No counterpart in the reference, which only times whole
  * runs with host std::chrono (src/algorithm/gpu/bfs.cu:70,93-95).  While
  * tracing is enabled on a handle, traversals run level by level from the

@@ -135,3 +135,34 @@ def test_heavy_pull_rows():
     assert g.degrees().max() > 20000
     srcs = gen.sources(g, 130, seed=15)
     check(g, srcs, variants=[abi.VARIANT_BITSET])
+
+
+@pytest.mark.parametrize("width", [1, 2, 4])
+def test_bitset_widths(width):
+    # every batch width gives the same distances; 300 sources leave a ragged
+    # last batch at each width
+    g = gen.rmat(15, 16, seed=21)
+    srcs = gen.sources(g, 300, seed=22)
+    want, edges = expected(g, srcs)
+    with abi.Graph(g) as dg:
+        dg.set_option(abi.OPT_BITSET_WIDTH, width)
+        assert dg.get_option(abi.OPT_BITSET_WIDTH) == width
+        for ratio in (1, 4, 64):
+            dg.set_option(abi.OPT_PUSH_RATIO, ratio)
+            d, st = dg.bfs(srcs, variant=abi.VARIANT_BITSET)
+            assert np.array_equal(d, want), (width, ratio)
+            assert st.edges_traversed == edges
+            assert st.batches == -(-len(srcs) // (64 * width))
+
+
+def test_width_changes_on_one_handle():
+    # a wider batch grows the handle's buffers; narrower widths run after it
+    # must not use the buffers of before
+    g = gen.rmat(14, 8, seed=23)
+    srcs = gen.sources(g, 260, seed=24)
+    want, _ = expected(g, srcs)
+    with abi.Graph(g) as dg:
+        for width, k in ((1, 40), (4, 260), (1, 40), (2, 130), (0, 260), (1, 64)):
+            dg.set_option(abi.OPT_BITSET_WIDTH, width)
+            d, _ = dg.bfs(srcs[:k], variant=abi.VARIANT_BITSET)
+            assert np.array_equal(d, want[:k]), (width, k)

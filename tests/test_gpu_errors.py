@@ -42,3 +42,15 @@ def test_bad_sources_rejected():
         # the handle stays usable after rejected calls
         d, _ = dg.bfs([0])
         assert d[0, 0] == 0
+
+
+def test_bad_options_rejected():
+    g = gen.rmat(8, 4, seed=2)
+    with abi.Graph(g) as dg:
+        for opt, val in ((abi.OPT_BITSET_WIDTH, 3), (abi.OPT_BITSET_WIDTH, 8), (abi.OPT_PUSH_RATIO, 0),
+                         (99, 1)):
+            with pytest.raises(abi.DawnError) as e:
+                dg.set_option(opt, val)
+            assert e.value.status == abi.ERR_INVALID_ARG
+        assert dg.get_option(abi.OPT_BITSET_WIDTH) == 0
+        assert dg.get_option(abi.OPT_PUSH_RATIO) == 4
