@@ -480,6 +480,12 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, 
   return s;
 }
 
+dawn_status dawn_bfs_static(const int32_t* row_ptr, const int32_t* col, int32_t n, int64_t m, int32_t source,
+                            int32_t* dist, uint32_t flags, void* stream) {
+  dawn::clear_error();
+  return dawn::bfs_static(row_ptr, col, n, m, source, dist, flags, static_cast<cudaStream_t>(stream));
+}
+
 dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value) {
   dawn::clear_error();
   if (!g) {

@@ -15,6 +15,8 @@
 // alpha/beta rule) on the device.  Both kernels emit the next frontier as a
 // queue and as a bitmap, so either direction can follow.  Distances are
 // written once, when a vertex is claimed.
+#include <mutex>
+
 #include "dawn_device.cuh"
 
 namespace dawn {
@@ -313,6 +315,199 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   fam.in_graph = &a.in_graph;
   fam.done_flag = &a.ctl->done;
   return ss_run(g, fam, nsrc, &g->bfs_exec);
+}
+
+// --- single-source BFS with static scratch (dawn_bfs_static) ---------------
+//
+// Some callers may not allocate device memory at the moment they traverse:
+// a serving loop whose device memory is entirely reserved by another
+// allocator, or one that must never wait on the allocator (an allocation
+// can synchronise the device, or fail under fragmentation, at a point where
+// neither is acceptable).  For them the push traversal above runs over a
+// fixed block of device memory that the library declares at file scope, so
+// the call allocates nothing: the caller owns the CSR and the distance row,
+// and every other word the traversal touches lives in `g_static_scratch`.
+//
+// The block holds a graph of at most kStaticMaxVertices vertices and
+// kStaticMaxEdges edges (about 12.5 MiB); every GPU on which the library is
+// loaded keeps it until the process exits.  There is one block per device,
+// so calls that overlap on one device (from two host threads, or on two
+// streams) race on it: the caller serialises them.
+
+constexpr int32_t kStaticMaxVertices = DAWN_STATIC_MAX_VERTICES;
+constexpr long long kStaticMaxEdges = DAWN_STATIC_MAX_EDGES;
+constexpr size_t kStaticSegCap = 2 * (size_t)(kStaticMaxEdges / kSeg) + 64;  // seg_capacity at the maxima
+constexpr size_t kStaticWords = (size_t)(kStaticMaxVertices + 31) / 32;
+// layout (byte offsets, each 256-aligned): control block | source | flags |
+// 4 bitmaps | 2 vertex queues | 2 segment lists
+constexpr size_t kStaticCtlOff = 0;
+constexpr size_t kStaticSrcOff = 512;
+constexpr size_t kStaticFlagOff = 768;
+constexpr size_t kStaticBitmapOff = 1024;
+constexpr size_t kStaticQueueOff = kStaticBitmapOff + 4 * kStaticWords * sizeof(uint32_t);
+constexpr size_t kStaticSegOff = kStaticQueueOff + 2 * (size_t)kStaticMaxVertices * sizeof(int32_t);
+constexpr size_t kStaticBytes = kStaticSegOff + 2 * kStaticSegCap * sizeof(Seg);
+static_assert(sizeof(SsCtl) <= kStaticSrcOff, "control block overlaps the source slot");
+static_assert(kStaticQueueOff % 256 == 0 && kStaticSegOff % 256 == 0, "scratch regions must stay 256-aligned");
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+namespace {
+
+constexpr int kStaticPollLevels = 8;  // levels launched between two reads of the done flag
+constexpr int kStaticMaxDevices = 64;
+
+struct StaticDevice {
+  std::once_flag once;
+  cudaError_t err = cudaSuccess;
+  unsigned char* scratch = nullptr;
+  int clear_blocks = 0, push_blocks = 0, check_blocks = 0;
+};
+StaticDevice g_static_dev[kStaticMaxDevices];
+
+// Set-up of one device, run once with that device current: the address of
+// its copy of the scratch block and the launch shapes.
+void static_setup(StaticDevice& d) {
+  d.err = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.scratch), g_static_scratch);
+  if (d.err != cudaSuccess) return;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((d.err = cudaGetDevice(&dev)) != cudaSuccess) return;
+  if ((d.err = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return;
+  if ((d.err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bfs_push, kBlock, 0)) != cudaSuccess) return;
+  d.push_blocks = sms * (per_sm > 0 ? per_sm : 1);
+  d.clear_blocks = sms * 4;
+  d.check_blocks = sms * 8;
+}
+
+// CSR checks of the static path: same invariants as the upload-time
+// validation, with scalar loads (the caller's arrays carry no alignment
+// promise beyond 4 bytes).  Flags: 1 row_ptr[0] != 0, 2 row_ptr[n] != m,
+// 4 row_ptr decreases, 8 column outside [0, n).
+__global__ void __launch_bounds__(kBlock) static_check_csr(const int32_t* __restrict__ rp,
+                                                           const int32_t* __restrict__ col, int32_t n, long long m,
+                                                           int* __restrict__ flags) {
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  int f = 0;
+  if (tid == 0) {
+    if (rp[0] != 0) f |= 1;
+    if ((long long)rp[n] != m) f |= 2;
+  }
+  for (size_t i = tid; i < (size_t)n; i += stride)
+    if (rp[i] > rp[i + 1]) f |= 4;
+  for (size_t k = tid; k < (size_t)m; k += stride) {
+    const int32_t c = __ldg(col + k);
+    if (c < 0 || c >= n) f |= 8;
+  }
+  if (f) atomicOr(flags, f);
+}
+
+// Writes the control block of a one-source push traversal into the
+// scratch (every field, so nothing is left from an earlier call) and clears
+// the flag word.
+__global__ void static_begin(SsCtl* __restrict__ ctl, int32_t* __restrict__ src_slot, int* __restrict__ flags,
+                             int32_t source, int32_t* dist) {
+  if (threadIdx.x != 0) return;
+  SsCtl c = {};
+  c.policy = DAWN_VARIANT_PUSH;
+  c.nsrc = 1;
+  c.dist_base = dist;
+  c.sources = src_slot;
+  *ctl = c;
+  *src_slot = source;
+  *flags = 0;
+}
+
+}  // namespace
+
+dawn_status bfs_static(const int32_t* row_ptr, const int32_t* col, int32_t n, int64_t m, int32_t source,
+                       int32_t* dist, uint32_t flags, cudaStream_t stream) {
+  if (!row_ptr || !dist || (m > 0 && !col)) {
+    set_error("dawn_bfs_static: row_ptr, col and dist must be device pointers (col may be NULL only when m = 0)");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (n < 1 || n > kStaticMaxVertices) {
+    set_error("dawn_bfs_static: n = %d outside [1, %d], the vertex limit of the static scratch block", n,
+              kStaticMaxVertices);
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (m < 0 || m > kStaticMaxEdges) {
+    set_error("dawn_bfs_static: m = %lld outside [0, %lld], the edge limit of the static scratch block",
+              (long long)m, kStaticMaxEdges);
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (source < 0 || source >= n) {
+    set_error("dawn_bfs_static: source %d outside [0, %d)", source, n);
+    return DAWN_ERR_INVALID_ARG;
+  }
+  int dev = 0;
+  DAWN_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kStaticMaxDevices) {
+    set_error("dawn_bfs_static: device %d beyond the %d devices the library tracks", dev, kStaticMaxDevices);
+    return DAWN_ERR_UNSUPPORTED;
+  }
+  const void* ptrs[3] = {row_ptr, col, dist};
+  for (const void* p : ptrs) {
+    if (!p) continue;
+    cudaPointerAttributes at;
+    DAWN_CUDA(cudaPointerGetAttributes(&at, p));
+    if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) || at.device != dev) {
+      set_error("dawn_bfs_static: row_ptr, col and dist must be memory of the current device (%d)", dev);
+      return DAWN_ERR_INVALID_ARG;
+    }
+  }
+  StaticDevice& d = g_static_dev[dev];
+  std::call_once(d.once, static_setup, std::ref(d));
+  DAWN_CUDA(d.err);
+
+  SsCtl* ctl = reinterpret_cast<SsCtl*>(d.scratch + kStaticCtlOff);
+  int32_t* src_slot = reinterpret_cast<int32_t*>(d.scratch + kStaticSrcOff);
+  int* d_flags = reinterpret_cast<int*>(d.scratch + kStaticFlagOff);
+  uint32_t* bitmaps = reinterpret_cast<uint32_t*>(d.scratch + kStaticBitmapOff);
+  int32_t* q = reinterpret_cast<int32_t*>(d.scratch + kStaticQueueOff);
+  Seg* segs = reinterpret_cast<Seg*>(d.scratch + kStaticSegOff);
+  const int32_t nwords = (n + 31) / 32;
+  uint32_t* vbm = bitmaps;
+  uint32_t* fbm = bitmaps + nwords;
+
+  static_begin<<<1, 32, 0, stream>>>(ctl, src_slot, d_flags, source, dist);
+  DAWN_CUDA(cudaGetLastError());
+  if (!(flags & DAWN_GRAPH_NO_VALIDATE)) {
+    static_check_csr<<<d.check_blocks, kBlock, 0, stream>>>(row_ptr, col, n, (long long)m, d_flags);
+    DAWN_CUDA(cudaGetLastError());
+    int f = 0;
+    DAWN_CUDA(cudaMemcpyAsync(&f, d_flags, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    DAWN_CUDA(cudaStreamSynchronize(stream));
+    if (f) {
+      set_error("dawn_bfs_static: invalid CSR:%s%s%s%s", (f & 1) ? " row_ptr[0] != 0;" : "",
+                (f & 2) ? " row_ptr[n] != m;" : "", (f & 4) ? " row_ptr decreases;" : "",
+                (f & 8) ? " col index outside [0, n);" : "");
+      return DAWN_ERR_INVALID_ARG;
+    }
+  }
+  // bfs_clear fills the distance row with -1 and zeroes the visited and
+  // frontier bitmaps; bfs_init seeds the source.  Queues and segment lists
+  // are read only up to the sizes the control block records.
+  bfs_clear<<<d.clear_blocks, kBlock, 0, stream>>>(ctl, bitmaps, n, nwords);
+  DAWN_CUDA(cudaGetLastError());
+  bfs_init<<<1, 32, 0, stream>>>(ctl, row_ptr, q, segs, vbm, n, (long long)m);
+  DAWN_CUDA(cudaGetLastError());
+  // Levels after the last one return at once (done is set), so the host
+  // reads the flag only every kStaticPollLevels levels.  Each level sets
+  // done once its frontier is empty or the level count reaches n.
+  for (;;) {
+    for (int j = 0; j < kStaticPollLevels; j++) {
+      bfs_push<<<d.push_blocks, kBlock, 0, stream>>>(row_ptr, col, ctl, q, segs, kStaticSegCap, vbm, fbm, n,
+                                                      nwords);
+      bfs_decide<<<1, 32, 0, stream>>>(ctl, n, 0, 0);
+    }
+    DAWN_CUDA(cudaGetLastError());
+    int32_t done = 0;
+    DAWN_CUDA(cudaMemcpyAsync(&done, &ctl->done, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    DAWN_CUDA(cudaStreamSynchronize(stream));
+    if (done) break;
+  }
+  return DAWN_OK;
 }
 
 }  // namespace dawn

@@ -198,6 +198,9 @@ namespace dawn {
 // bovm.cu
 dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                        int32_t* d_dist, int32_t policy);
+dawn_status bfs_static(const int32_t* row_ptr, const int32_t* col, int32_t n,
+                       int64_t m, int32_t source, int32_t* dist, uint32_t flags,
+                       cudaStream_t stream);
 // msbfs.cu
 dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                        int32_t* d_dist);

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libdawn_gb300.so")
 
 # Every symbol the header declares; tests check the library exports them.
 EXPORTS = ("dawn_graph_create", "dawn_graph_create_device", "dawn_graph_destroy",
-           "dawn_graph_set_stream", "dawn_graph_synchronize", "dawn_bfs", "dawn_bfs_device",
+           "dawn_graph_set_stream", "dawn_graph_synchronize", "dawn_bfs", "dawn_bfs_device", "dawn_bfs_static",
            "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_graph_set_option",
            "dawn_graph_get_option", "dawn_trace_enable", "dawn_trace_read", "dawn_last_error", "dawn_version")
 OPT_BITSET_WIDTH, OPT_PUSH_RATIO = 1, 2
@@ -72,6 +72,8 @@ def lib():
         L.dawn_graph_synchronize.argtypes = [_VP]
         L.dawn_bfs.argtypes = [_VP, _VP, ctypes.c_int32, _VP, ctypes.c_int32, ctypes.POINTER(Stats)]
         L.dawn_bfs_device.argtypes = L.dawn_bfs.argtypes
+        L.dawn_bfs_static.argtypes = [_VP, _VP, ctypes.c_int32, ctypes.c_int64, ctypes.c_int32, _VP,
+                                      ctypes.c_uint32, _VP]
         L.dawn_sssp.argtypes = L.dawn_bfs.argtypes
         L.dawn_sssp_device.argtypes = L.dawn_bfs.argtypes
         L.dawn_closeness.argtypes = [_VP, _VP, ctypes.c_int32, ctypes.c_int32, _VP, _VP, _VP,
@@ -241,6 +243,18 @@ class Graph:
         _check(lib().dawn_sssp_device(self.handle, _ptr(s), len(s), ctypes.c_void_p(d_dist), 0,
                                       ctypes.byref(st) if st is not None else None))
         return st
+
+
+STATIC_MAX_VERTICES, STATIC_MAX_EDGES = 1 << 20, 1 << 24
+
+
+def bfs_static(row_ptr, col, n, m, source, dist, flags=0, stream=None):
+    """dawn_bfs_static: hop distances from one source into `dist`, with the
+    CSR and `dist` given as device addresses (ints) of the current device.
+    Allocates nothing; graphs beyond STATIC_MAX_VERTICES / STATIC_MAX_EDGES
+    raise DawnError.  Calls that overlap on one device race."""
+    _check(lib().dawn_bfs_static(ctypes.c_void_p(row_ptr), ctypes.c_void_p(col), n, m, source,
+                                 ctypes.c_void_p(dist), flags, ctypes.c_void_p(stream)))
 
 
 def version():

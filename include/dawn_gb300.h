@@ -111,6 +111,33 @@ dawn_status dawn_bfs_device(dawn_graph* g, const int32_t* sources,
                             int32_t nsrc, int32_t* d_dist, int32_t variant,
                             dawn_stats* stats);
 
+/* Single-source hop distances that allocate nothing (no counterpart in
+ * the reference: every reference driver allocates its own device arrays per
+ * call, src/algorithm/gpu/bfs.cu:36-46).  For callers that may not allocate
+ * while they traverse: a serving loop whose device memory is owned entirely
+ * by another allocator, or one that must not wait on an allocation, which
+ * can synchronise the device or fail under fragmentation.
+ *   row_ptr (n + 1), col (m) and dist (n) are memory of the calling
+ *   thread's current device; no handle is needed.  dist receives the hop
+ *   distance of every vertex from source, -1 where unreachable: the same
+ *   values as dawn_bfs / dawn_bfs_device on a handle of the same CSR.
+ *   Top-down (push) levels only.  flags: DAWN_GRAPH_NO_VALIDATE skips the
+ *   CSR check that otherwise runs first.  stream orders the work (NULL: the
+ *   default stream); the call returns once the traversal has finished.
+ * Working memory is one fixed block of device memory per GPU, declared by
+ * the library (about 12.5 MiB, held on every GPU where the library is
+ * loaded until the process exits), so a graph is limited to
+ * DAWN_STATIC_MAX_VERTICES vertices and DAWN_STATIC_MAX_EDGES edges; larger
+ * ones are rejected with DAWN_ERR_INVALID_ARG.  The first call on a device
+ * looks up that device's block; make it before any stream capture.  Calls
+ * that overlap on one device (two host threads, or two streams) share the
+ * block and race: serialise them. */
+#define DAWN_STATIC_MAX_VERTICES (1 << 20)
+#define DAWN_STATIC_MAX_EDGES (1LL << 24)
+dawn_status dawn_bfs_static(const int32_t* row_ptr, const int32_t* col,
+                            int32_t n, int64_t m, int32_t source,
+                            int32_t* dist, uint32_t flags, void* stream);
+
 /* Weighted shortest-path distances (min-plus relax).  dist is nsrc x n of
  * int32 (DAWN_W_I32 graphs) or float (DAWN_W_F32 graphs).  Replaces
  * SSSP_GPU::kernel + GOVM (src/algorithm/gpu/sssp.cu:18-129) and
