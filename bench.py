@@ -277,7 +277,9 @@ def suite_lines(torch, abi, gen, stream, rank):
     """The other workload shapes, one JSON line each (not the headline line):
     directed ER n=65,536 x 64 sources (the CPU-runnable case), weighted
     SSSP on the RMAT-22 topology x 64 sources (int32 and float32 weights),
-    and RMAT-18 x 4,096 sources."""
+    RMAT-18 x 4,096 sources, and 512 uneven directed ER graphs (n in
+    [1,024, 65,536], average degree in [4, 32], 8-64 sources each) in one
+    persistent launch."""
     out = []
 
     def timed(fn, steps=3):
@@ -327,6 +329,33 @@ def suite_lines(torch, abi, gen, stream, rank):
         st2 = dg.bfs_device(srcs[:256], d.data_ptr(), variant=abi.VARIANT_DO)
         out.append({"suite": "rmat18-bfs-4096src", "variant": "plain (first 256 sources)",
                     "ms_per_step": round(ms, 3), "gteps": round(st2.edges_traversed / (ms * 1e-3) / 1e9, 2)})
+    del g, d
+    # 512 independent directed ER graphs, 8-64 sources each, one persistent launch
+    graphs, gsrcs = gen.er_family(ngraphs=512, seed=GRAPH_SEED)
+    u, off = gen.disjoint_union(graphs)
+    with abi.Graph(u, stream=stream) as dg:
+        dg.set_parts(off)
+        d = torch.empty(dg.multi_out_size(gsrcs), dtype=torch.int32, device="cuda")
+        st = dg.multi_bfs_ptr(gsrcs, d.data_ptr(), device=True)
+        ms = timed(lambda: dg.multi_bfs_ptr(gsrcs, d.data_ptr(), device=True, stats=False), 5)
+        out.append({"suite": "er512-multi-graph-bfs", "variant": "one persistent launch", "ms_per_step": round(ms, 3),
+                    "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2), "graphs": len(graphs),
+                    "sources": int(sum(len(x) for x in gsrcs)), "n_total": u.n, "m_total": u.m,
+                    "levels": st.levels, "tasks": st.batches})
+    del u, d
+    # the same graphs one at a time (first 32): batched bitset per graph, and
+    # the plain single-source traversal per (graph, source)
+    sub = 32
+    for var, name in ((abi.VARIANT_BITSET, "per-graph bitset"), (abi.VARIANT_DO, "per-graph plain")):
+        tot_ms, tot_edges = 0.0, 0
+        for g1, s1 in zip(graphs[:sub], gsrcs[:sub]):
+            with abi.Graph(g1, stream=stream) as dg:
+                d = torch.empty((len(s1), g1.n), dtype=torch.int32, device="cuda")
+                st = dg.bfs_device(s1, d.data_ptr(), variant=var)
+                tot_ms += timed(lambda: dg.bfs_device(s1, d.data_ptr(), variant=var, stats=False), 1)
+                tot_edges += st.edges_traversed
+        out.append({"suite": "er512-multi-graph-bfs", "variant": f"{name} (first {sub} graphs)",
+                    "ms_per_step": round(tot_ms, 3), "gteps": round(tot_edges / (tot_ms * 1e-3) / 1e9, 2)})
     if rank == 0:
         for line in out:
             print(json.dumps(line), flush=True)

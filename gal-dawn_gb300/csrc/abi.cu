@@ -89,13 +89,14 @@ void destroy(dawn_graph* g) {
   if (g->val) dawn::pool_free(g->val, g->stream);
   DevBuf* bufs[] = {&g->ss_queues, &g->ss_segs, &g->bs_segs, &g->ss_bitmaps, &g->ss_ctl, &g->ss_sources, &g->ss_scratch,
                     &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
-                    &g->dist_stage};
+                    &g->dist_stage, &g->pt_voff, &g->pt_tasks, &g->pt_sources, &g->pt_ctl, &g->pt_scratch, &g->pt_rows};
   for (DevBuf* b : bufs) dawn::release(*b);
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
   if (g->sssp_exec) cudaGraphExecDestroy(g->sssp_exec);
   for (cudaGraphExec_t e : g->bs_exec)
     if (e) cudaGraphExecDestroy(e);
+  if (g->pt_exec) cudaGraphExecDestroy(g->pt_exec);
   if (g->h_ctl) cudaFreeHost(g->h_ctl);
   for (cudaEvent_t e : g->trace_ev)
     if (e) cudaEventDestroy(e);
@@ -224,6 +225,40 @@ dawn_status staged(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* ho
     if (st) add_stats(st, s);
   }
   DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  return DAWN_OK;
+}
+
+long long multi_out_elems(const dawn_graph* g, const int32_t* source_offset) {
+  long long out = 0;
+  const int32_t nparts = (int32_t)g->pt_off.size() - 1;
+  for (int32_t p = 0; p < nparts; p++)
+    out += (long long)(source_offset[p + 1] - source_offset[p]) * (g->pt_off[p + 1] - g->pt_off[p]);
+  return out;
+}
+
+dawn_status multi_args(const dawn_graph* g, const int32_t* source_offset, const int32_t* sources) {
+  if (!g || !source_offset) {
+    dawn::set_error("graph or source_offset is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (g->pt_off.size() < 2) {
+    dawn::set_error("the graph has no parts: call dawn_graph_set_parts first");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  const int32_t nparts = (int32_t)g->pt_off.size() - 1;
+  if (source_offset[0] != 0) {
+    dawn::set_error("source_offset[0] must be 0");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  for (int32_t p = 0; p < nparts; p++)
+    if (source_offset[p + 1] < source_offset[p]) {
+      dawn::set_error("source_offset decreases at part %d", p);
+      return DAWN_ERR_INVALID_ARG;
+    }
+  if (source_offset[nparts] > 0 && !sources) {
+    dawn::set_error("sources is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
   return DAWN_OK;
 }
 
@@ -478,6 +513,90 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, 
   }
   dawn::release(srcbuf);
   return s;
+}
+
+dawn_status dawn_graph_set_parts(dawn_graph* g, int32_t nparts, const int32_t* offsets) {
+  dawn::clear_error();
+  if (!g) {
+    dawn::set_error("graph is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  return dawn::parts_set(g, nparts, offsets);
+}
+
+dawn_status dawn_multi_bfs_device(dawn_graph* g, const int32_t* source_offset, const int32_t* sources,
+                                  int32_t* d_dist, dawn_stats* stats) {
+  dawn::clear_error();
+  DAWN_CHECK(multi_args(g, source_offset, sources));
+  if (!d_dist && multi_out_elems(g, source_offset) > 0) {
+    dawn::set_error("dist is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (stats) DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
+  DAWN_CHECK(dawn::parts_bfs(g, source_offset, sources, d_dist, nullptr, stats));
+  if (stats) {
+    DAWN_CUDA(cudaEventRecord(g->ev1, g->stream));
+    DAWN_CUDA(cudaEventSynchronize(g->ev1));
+    DAWN_CUDA(cudaEventElapsedTime(&stats->device_ms, g->ev0, g->ev1));
+  }
+  return DAWN_OK;
+}
+
+dawn_status dawn_multi_bfs(dawn_graph* g, const int32_t* source_offset, const int32_t* sources, int32_t* dist,
+                           dawn_stats* stats) {
+  dawn::clear_error();
+  DAWN_CHECK(multi_args(g, source_offset, sources));
+  const long long elems = multi_out_elems(g, source_offset);
+  if (!dist && elems > 0) {
+    dawn::set_error("dist is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (elems == 0) return dawn_multi_bfs_device(g, source_offset, sources, nullptr, stats);
+  if (is_pinned_host(dist)) {
+    // distances are written once, by the final pass of each task: a
+    // page-locked buffer takes them directly
+    DAWN_CHECK(dawn_multi_bfs_device(g, source_offset, sources, dist, stats));
+    DAWN_CUDA(cudaStreamSynchronize(g->stream));
+    return DAWN_OK;
+  }
+  const size_t bytes = sizeof(int32_t) * (size_t)elems;
+  DAWN_CHECK(dawn::ensure(g->dist_stage, bytes, g->stream));
+  DAWN_CHECK(dawn_multi_bfs_device(g, source_offset, sources, g->dist_stage.as<int32_t>(), stats));
+  DAWN_CUDA(cudaMemcpyAsync(dist, g->dist_stage.p, bytes, cudaMemcpyDeviceToHost, g->stream));
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  return DAWN_OK;
+}
+
+dawn_status dawn_multi_closeness(dawn_graph* g, const int32_t* source_offset, const int32_t* sources, double* cc,
+                                 double* dist_sum, int64_t* reached, dawn_stats* stats) {
+  dawn::clear_error();
+  DAWN_CHECK(multi_args(g, source_offset, sources));
+  const int32_t nparts = (int32_t)g->pt_off.size() - 1;
+  const int32_t nsrc = source_offset[nparts];
+  if (nsrc > 0 && !cc) {
+    dawn::set_error("cc is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  const long long elems = multi_out_elems(g, source_offset);
+  if (elems == 0) return dawn_multi_bfs_device(g, source_offset, sources, nullptr, stats);
+  DAWN_CHECK(dawn::ensure(g->dist_stage, sizeof(int32_t) * (size_t)elems, g->stream));
+  std::vector<dawn::PartRow> rows;
+  if (stats) DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
+  DAWN_CHECK(dawn::parts_bfs(g, source_offset, sources, g->dist_stage.as<int32_t>(), &rows, stats));
+  std::vector<long long> hs(rows.size()), hc(rows.size());
+  DAWN_CHECK(dawn::parts_row_reduce(g, g->dist_stage.as<int32_t>(), rows, hs.data(), hc.data()));
+  if (stats) {
+    DAWN_CUDA(cudaEventRecord(g->ev1, g->stream));
+    DAWN_CUDA(cudaEventSynchronize(g->ev1));
+    DAWN_CUDA(cudaEventElapsedTime(&stats->device_ms, g->ev0, g->ev1));
+  }
+  for (size_t i = 0; i < rows.size(); i++) {
+    const double total = (double)hs[i];
+    cc[i] = total > 0 ? (double)(rows[i].len - 1) / total : 0.0;
+    if (dist_sum) dist_sum[i] = total;
+    if (reached) reached[i] = hc[i];
+  }
+  return DAWN_OK;
 }
 
 dawn_status dawn_bfs_static(const int32_t* row_ptr, const int32_t* col, int32_t n, int64_t m, int32_t source,

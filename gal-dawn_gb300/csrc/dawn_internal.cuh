@@ -122,6 +122,22 @@ struct SsFamily {
   void (*probe)(const void* ctl, LevelProbe* out) = nullptr;
 };
 
+// One task of the multi-graph traversal: up to 64 sources of one part.
+struct PartTask {
+  int32_t part;    // part index
+  int32_t src0;    // first source, an index into the call's source list
+  int32_t nsrc;    // sources in the task (1..64)
+  int32_t pad;
+  long long out0;  // output offset of the task's first distance row
+};
+// One distance row of the multi-graph output (closeness reduction).
+struct PartRow {
+  long long off;   // output offset
+  int32_t len;     // the part's vertex count
+  int32_t part;
+};
+constexpr int32_t kPartMaxVertices = DAWN_PART_MAX_VERTICES;
+
 // Launch geometry for persistent grids on this device.
 struct Geometry {
   int sms = 0;
@@ -173,6 +189,14 @@ struct dawn_graph {
   int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges
   int32_t bs_width = 0;         // words per vertex of the bitset traversal (0 = by source count)
 
+  // disjoint-union parts (dawn_graph_set_parts)
+  std::vector<int32_t> pt_off;   // nparts + 1 vertex offsets (empty: no parts)
+  std::vector<long long> pt_pos; // row_ptr at those offsets (edge positions)
+  dawn::DevBuf pt_voff, pt_tasks, pt_sources, pt_ctl, pt_scratch, pt_rows;
+  size_t pt_slot_words = 0;
+  int32_t pt_slots = 0, pt_maxn = 0;
+  cudaGraphExec_t pt_exec = nullptr;
+
   // closeness reduction
   dawn::DevBuf cc_out;
 
@@ -198,6 +222,15 @@ namespace dawn {
 // bovm.cu
 dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                        int32_t* d_dist, int32_t policy);
+// parts.cu
+dawn_status parts_set(dawn_graph* g, int32_t nparts, const int32_t* offsets);
+dawn_status parts_bfs(dawn_graph* g, const int32_t* source_offset,
+                      const int32_t* sources, int32_t* d_dist,
+                      std::vector<PartRow>* rows_out, dawn_stats* st);
+dawn_status parts_row_reduce(dawn_graph* g, const int32_t* d_dist,
+                             const std::vector<PartRow>& rows, long long* h_sum,
+                             long long* h_cnt);
+
 dawn_status bfs_static(const int32_t* row_ptr, const int32_t* col, int32_t n,
                        int64_t m, int32_t source, int32_t* dist, uint32_t flags,
                        cudaStream_t stream);

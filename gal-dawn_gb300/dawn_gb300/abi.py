@@ -24,7 +24,8 @@ LIB_PATH = os.path.join(LIB_DIR, "libdawn_gb300.so")
 EXPORTS = ("dawn_graph_create", "dawn_graph_create_device", "dawn_graph_destroy",
            "dawn_graph_set_stream", "dawn_graph_synchronize", "dawn_bfs", "dawn_bfs_device", "dawn_bfs_static",
            "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_graph_set_option",
-           "dawn_graph_get_option", "dawn_trace_enable", "dawn_trace_read", "dawn_last_error", "dawn_version")
+           "dawn_graph_get_option", "dawn_graph_set_parts", "dawn_multi_bfs", "dawn_multi_bfs_device",
+           "dawn_multi_closeness", "dawn_trace_enable", "dawn_trace_read", "dawn_last_error", "dawn_version")
 OPT_BITSET_WIDTH, OPT_PUSH_RATIO = 1, 2
 
 
@@ -80,6 +81,10 @@ def lib():
                                      ctypes.POINTER(Stats)]
         L.dawn_graph_set_option.argtypes = [_VP, ctypes.c_int32, ctypes.c_int64]
         L.dawn_graph_get_option.argtypes = [_VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
+        L.dawn_graph_set_parts.argtypes = [_VP, ctypes.c_int32, _VP]
+        L.dawn_multi_bfs.argtypes = [_VP, _VP, _VP, _VP, ctypes.POINTER(Stats)]
+        L.dawn_multi_bfs_device.argtypes = L.dawn_multi_bfs.argtypes
+        L.dawn_multi_closeness.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, ctypes.POINTER(Stats)]
         L.dawn_trace_enable.argtypes = [_VP, ctypes.c_int32]
         L.dawn_trace_read.argtypes = [_VP, ctypes.POINTER(TraceRec), ctypes.c_int64,
                                       ctypes.POINTER(ctypes.c_int64)]
@@ -186,6 +191,56 @@ class Graph:
         _check(lib().dawn_graph_get_option(self.handle, option, ctypes.byref(v)))
         return v.value
 
+    def set_parts(self, offsets):
+        """dawn_graph_set_parts: the graph is the disjoint union of the
+        vertex ranges [offsets[p], offsets[p+1])."""
+        self._parts = np.ascontiguousarray(offsets, np.int32)
+        _check(lib().dawn_graph_set_parts(self.handle, len(self._parts) - 1, _ptr(self._parts)))
+
+    def _multi_args(self, sources_per_part):
+        so = np.zeros(len(self._parts), np.int32)
+        so[1:] = np.cumsum([len(s) for s in sources_per_part])
+        src = (np.concatenate([np.asarray(s, np.int32) for s in sources_per_part]) if len(sources_per_part)
+               else np.zeros(0, np.int32))
+        return so, np.ascontiguousarray(src, np.int32)
+
+    def multi_out_size(self, sources_per_part):
+        sizes = np.diff(self._parts.astype(np.int64))
+        return int(sum(len(s) * int(sizes[p]) for p, s in enumerate(sources_per_part)))
+
+    def multi_bfs(self, sources_per_part, out=None):
+        """dawn_multi_bfs: returns (list of per-part (sources x n_p) blocks, stats)."""
+        so, src = self._multi_args(sources_per_part)
+        d = out if out is not None else np.empty(self.multi_out_size(sources_per_part), np.int32)
+        st = Stats()
+        _check(lib().dawn_multi_bfs(self.handle, _ptr(so), _ptr(src), _ptr(d), ctypes.byref(st)))
+        blocks, o = [], 0
+        sizes = np.diff(self._parts.astype(np.int64))
+        for p, s in enumerate(sources_per_part):
+            k, npart = len(s), int(sizes[p])
+            blocks.append(d[o:o + k * npart].reshape(k, npart))
+            o += k * npart
+        return blocks, st
+
+    def multi_bfs_ptr(self, sources_per_part, dist_ptr, device=False, stats=True):
+        """dawn_multi_bfs (host pointer) or dawn_multi_bfs_device into a raw buffer."""
+        so, src = self._multi_args(sources_per_part)
+        st = Stats() if stats else None
+        fn = lib().dawn_multi_bfs_device if device else lib().dawn_multi_bfs
+        _check(fn(self.handle, _ptr(so), _ptr(src), ctypes.c_void_p(dist_ptr),
+                  ctypes.byref(st) if st is not None else None))
+        return st
+
+    def multi_closeness(self, sources_per_part):
+        so, src = self._multi_args(sources_per_part)
+        cc = np.empty(len(src), np.float64)
+        ds = np.empty(len(src), np.float64)
+        rc = np.empty(len(src), np.int64)
+        st = Stats()
+        _check(lib().dawn_multi_closeness(self.handle, _ptr(so), _ptr(src), _ptr(cc), _ptr(ds), _ptr(rc),
+                                          ctypes.byref(st)))
+        return cc, ds, rc, st
+
     def trace(self, enable=True):
         _check(lib().dawn_trace_enable(self.handle, int(enable)))
 
@@ -246,6 +301,7 @@ class Graph:
 
 
 STATIC_MAX_VERTICES, STATIC_MAX_EDGES = 1 << 20, 1 << 24
+PART_MAX_VERTICES = 1 << 18
 
 
 def bfs_static(row_ptr, col, n, m, source, dist, flags=0, stream=None):

@@ -152,3 +152,46 @@ def write_mtx(g: CsrGraph, path: str, weighted=False):
     c, keep = _as_csr_struct(g)
     _check(lib().dawn_write_mtx(ctypes.byref(c), path.encode(), int(g.symmetric),
                                 int(weighted)), "dawn_write_mtx")
+
+
+def disjoint_union(graphs):
+    """One CSR holding ``graphs`` side by side: vertex v of part p becomes
+    offsets[p] + v.  Returns (CsrGraph, int32 offsets[nparts + 1])."""
+    ns = np.array([g.n for g in graphs], np.int64)
+    ms = np.array([g.m for g in graphs], np.int64)
+    voff = np.concatenate([[0], np.cumsum(ns)])
+    eoff = np.concatenate([[0], np.cumsum(ms)])
+    if voff[-1] >= 2**31 or eoff[-1] >= 2**31:
+        raise ValueError("the union exceeds int32 vertex or edge ids")
+    rp = np.empty(int(voff[-1]) + 1, np.int32)
+    col = np.empty(int(eoff[-1]), np.int32)
+    weighted = all(g.w_i32 is not None for g in graphs)
+    wi = np.empty(int(eoff[-1]), np.int32) if weighted else None
+    wf = np.empty(int(eoff[-1]), np.float32) if weighted else None
+    for p, g in enumerate(graphs):
+        rp[voff[p]:voff[p + 1]] = g.row_ptr[:-1] + eoff[p]
+        col[eoff[p]:eoff[p + 1]] = g.col + voff[p]
+        if weighted:
+            wi[eoff[p]:eoff[p + 1]] = g.w_i32
+            wf[eoff[p]:eoff[p + 1]] = g.w_f32
+    rp[-1] = eoff[-1]
+    u = CsrGraph(int(voff[-1]), rp, col, wi, wf, symmetric=all(g.symmetric for g in graphs),
+                 name=f"union{len(graphs)}")
+    return u, voff.astype(np.int32)
+
+
+def er_family(ngraphs=512, nmin=1024, nmax=65536, dmin=4, dmax=32, smin=8, smax=64, seed=1):
+    """Independent directed Erdos-Renyi graphs with n uniform in [nmin, nmax],
+    average out-degree uniform in [dmin, dmax] and smin..smax sources each
+    (drawn uniformly, with the generator's seeds derived from ``seed``).
+    Returns (graphs, list of int32 source arrays)."""
+    rng = np.random.default_rng(seed)
+    graphs, srcs = [], []
+    for i in range(ngraphs):
+        n = int(rng.integers(nmin, nmax + 1))
+        d = float(rng.uniform(dmin, dmax))
+        g = erdos_renyi(n, int(round(n * d)), seed=int(rng.integers(1, 2**62)))
+        graphs.append(g)
+        k = int(rng.integers(smin, smax + 1))
+        srcs.append(rng.integers(0, n, size=k).astype(np.int32))
+    return graphs, srcs

@@ -138,6 +138,40 @@ dawn_status dawn_bfs_static(const int32_t* row_ptr, const int32_t* col,
                             int32_t n, int64_t m, int32_t source,
                             int32_t* dist, uint32_t flags, void* stream);
 
+/* Many independent graphs in one call (no counterpart in the reference,
+ * which traverses one graph per MSSP_GPU::run, src/algorithm/gpu/mssp.cu:9-51).
+ * The handle's graph is declared the disjoint union of nparts graphs:
+ * part p owns the vertices [offsets[p], offsets[p+1]) (offsets: host,
+ * nparts + 1 entries, from 0 to n) and no edge may leave its part (checked
+ * unless the handle was created with DAWN_GRAPH_NO_VALIDATE).  A part holds
+ * at most DAWN_PART_MAX_VERTICES vertices. */
+#define DAWN_PART_MAX_VERTICES (1 << 18)
+dawn_status dawn_graph_set_parts(dawn_graph* g, int32_t nparts,
+                                 const int32_t* offsets);
+
+/* Hop distances from the sources of every part, all parts in one
+ * persistent launch.  source_offset (host, nparts + 1, from 0) delimits
+ * each part's sources in `sources`, which hold part-local vertex ids.  dist
+ * receives, part after part, a (sources of p) x (vertices of p) int32 block
+ * in part-local ids, -1 where unreachable: the values dawn_bfs gives on
+ * each part as a graph of its own.  stats->batches counts the
+ * (part, 64-source) tasks. */
+dawn_status dawn_multi_bfs(dawn_graph* g, const int32_t* source_offset,
+                           const int32_t* sources, int32_t* dist,
+                           dawn_stats* stats);
+dawn_status dawn_multi_bfs_device(dawn_graph* g, const int32_t* source_offset,
+                                  const int32_t* sources, int32_t* d_dist,
+                                  dawn_stats* stats);
+
+/* Closeness of each (part, source): (n_p - 1) / sum of the hop distances
+ * to the vertices the source reaches in its part, as dawn_closeness
+ * computes it on the part alone.  cc, dist_sum and reached are indexed like
+ * `sources`; dist_sum and reached may be NULL. */
+dawn_status dawn_multi_closeness(dawn_graph* g, const int32_t* source_offset,
+                                 const int32_t* sources, double* cc,
+                                 double* dist_sum, int64_t* reached,
+                                 dawn_stats* stats);
+
 /* Weighted shortest-path distances (min-plus relax).  dist is nsrc x n of
  * int32 (DAWN_W_I32 graphs) or float (DAWN_W_F32 graphs).  Replaces
  * SSSP_GPU::kernel + GOVM (src/algorithm/gpu/sssp.cu:18-129) and
