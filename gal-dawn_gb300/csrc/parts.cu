@@ -53,11 +53,38 @@ struct PartsCtl {
   int32_t* dist;           // output base
   unsigned long long reached;  // TEPS numerator, all tasks
   unsigned long long levels, push_levels, pull_levels;
+  unsigned long long* task_log;  // tracing: 4 words per task, else NULL
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned sm_id() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
 
 __device__ __forceinline__ u64 block_reduce_add(u64 x, u64* s_slot) {
   x = warp_sum(x);
   if (lane_id() == 0 && x) atomicAdd(s_slot, x);
+  return x;
+}
+
+// Inclusive OR-scan of x over runs of lanes with equal key (keys must not
+// decrease from lane to lane): the last lane of a run ends with the OR of
+// the run.
+__device__ __forceinline__ u64 seg_or_scan(u64 x, int key) {
+  const int lane = lane_id();
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const u64 y = __shfl_up_sync(kFull, x, d);
+    const int ky = __shfl_up_sync(kFull, key, d);
+    if (lane >= d && ky == key) x |= y;
+  }
   return x;
 }
 
@@ -96,7 +123,11 @@ __global__ void __launch_bounds__(kPartBlock, 2) parts_traverse(PartsCtl* __rest
                                                            int32_t maxn) {
   __shared__ int s_task;
   __shared__ u64 s_mf, s_dec, s_nf;
+  __shared__ int s_excl[kPartBlock / 32][32];
+  __shared__ int s_rs[kPartBlock / 32][32];
+  __shared__ u64 s_w[kPartBlock / 32][32];
   const int tid = threadIdx.x;
+  const int lane = lane_id(), wib = tid >> 5;
   u64* const visit = scratch + (size_t)blockIdx.x * slot_words;
   u64* const fa = visit + maxn;
   u64* const fb = fa + maxn;
@@ -118,6 +149,8 @@ __global__ void __launch_bounds__(kPartBlock, 2) parts_traverse(PartsCtl* __rest
     const u64 full = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
     const int32_t* src = ctl->sources + task.src0;
     const long long mp = (long long)row_ptr[v0 + np] - row_ptr[v0];
+    unsigned long long t_start = 0, push0 = t_push;
+    if (tid == 0 && ctl->task_log) t_start = global_ns();
     if (tid == 0) {
       s_mf = 0;
       s_dec = 0;
@@ -157,37 +190,140 @@ __global__ void __launch_bounds__(kPartBlock, 2) parts_traverse(PartsCtl* __rest
         s_nf = 0;
       }
       if (push) {
-        for (int v = tid; v < np; v += kPartBlock) {
-          const u64 f = cur[v];
-          if (!f) continue;
-          const int e = row_ptr[v0 + v + 1];
-          for (int k = row_ptr[v0 + v]; k < e; k++) {
-            const int u = __ldg(col + k) - v0;
-            const u64 bits = f & ~visit[u];
+        // scatter: the frontier rows of 32 consecutive vertices per warp
+        // task; rows of >= kWarpRow entries swept by the whole warp, shorter
+        // ones concatenated across the lanes (coalesced col loads, 32
+        // independent visited loads in flight)
+        for (int base = wib * 32; base < np; base += kPartBlock) {
+          const int v = base + lane;
+          const u64 f = v < np ? cur[v] : 0ull;
+          int rs = 0, re = 0;
+          if (f) {
+            rs = row_ptr[v0 + v];
+            re = row_ptr[v0 + v + 1];
+          }
+          const int deg = re - rs;
+          if (__ballot_sync(kFull, deg > 0) == 0u) continue;
+          uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
+          while (big) {
+            const int leader = __ffs(big) - 1;
+            big &= big - 1;
+            const u64 lf = __shfl_sync(kFull, f, leader);
+            const int ks = __shfl_sync(kFull, rs, leader), ke = __shfl_sync(kFull, re, leader);
+            for (int k = ks + lane; k < ke; k += 32) {
+              const int u = __ldg(col + k) - v0;
+              const u64 bits = lf & ~visit[u];
+              if (bits) atomicOr(acc + u, bits);
+            }
+          }
+          const int sdeg = deg < kWarpRow ? deg : 0;
+          const int incl = warp_incl_scan(sdeg);
+          const int total = __shfl_sync(kFull, incl, 31);
+          s_excl[wib][lane] = incl - sdeg;
+          s_rs[wib][lane] = rs;
+          s_w[wib][lane] = f;
+          __syncwarp();
+          for (int e = lane; e < total; e += 32) {
+            int lo = 0, hi = 31;
+#pragma unroll
+            for (int it = 0; it < 5; it++) {
+              const int mid = (lo + hi + 1) >> 1;
+              if (s_excl[wib][mid] <= e) lo = mid; else hi = mid - 1;
+            }
+            const int u = __ldg(col + s_rs[wib][lo] + (e - s_excl[wib][lo])) - v0;
+            const u64 bits = s_w[wib][lo] & ~visit[u];
             if (bits) atomicOr(acc + u, bits);
           }
+          __syncwarp();
         }
       }
       __syncthreads();
       u64 lmf = 0, ldec = 0, lnf = 0;
-      for (int u = tid; u < np; u += kPartBlock) {
-        const u64 vis = visit[u];
+      for (int base = wib * 32; base < np; base += kPartBlock) {
+        const int u = base + lane;
+        const bool in = u < np;
+        const u64 vis = in ? visit[u] : full;
         u64 nw = 0ull;
         if (push) {
-          const u64 x = acc[u];
-          if (x) {
-            acc[u] = 0ull;
-            nw = x & ~vis;
+          if (in) {
+            const u64 x = acc[u];
+            if (x) {
+              acc[u] = 0ull;
+              nw = x & ~vis;
+            }
           }
-        } else if (vis != full) {
+        } else {
+          // pull: unfinished vertices OR their in-neighbours' frontier
+          // words; long rows by the whole warp with early exit, short rows
+          // concatenated and OR-ed into per-lane shared slots
+          const bool active = vis != full;
+          int rs = 0, re = 0;
+          if (active) {
+            rs = t_row_ptr[v0 + u];
+            re = t_row_ptr[v0 + u + 1];
+          }
+          const int deg = re - rs;
           u64 got = 0ull;
-          const int e = t_row_ptr[v0 + u + 1];
-          for (int k = t_row_ptr[v0 + u]; k < e; k++) {
-            got |= cur[__ldg(t_col + k) - v0];
-            if ((got | vis) == full) break;
+          uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
+          while (big) {
+            const int leader = __ffs(big) - 1;
+            big &= big - 1;
+            const u64 lvis = __shfl_sync(kFull, vis, leader);
+            const int ks = __shfl_sync(kFull, rs, leader), ke = __shfl_sync(kFull, re, leader);
+            u64 w = 0ull;
+            for (int k0 = ks; k0 < ke; k0 += 128) {
+              const int k = k0 + lane;
+              const int32_t c0 = k < ke ? __ldg(t_col + k) : -1;
+              const int32_t c1 = k + 32 < ke ? __ldg(t_col + k + 32) : -1;
+              const int32_t c2 = k + 64 < ke ? __ldg(t_col + k + 64) : -1;
+              const int32_t c3 = k + 96 < ke ? __ldg(t_col + k + 96) : -1;
+              if (c0 >= 0) w |= cur[c0 - v0];
+              if (c1 >= 0) w |= cur[c1 - v0];
+              if (c2 >= 0) w |= cur[c2 - v0];
+              if (c3 >= 0) w |= cur[c3 - v0];
+              if ((warp_or(w) | lvis) == full) break;
+            }
+            w = warp_or(w);
+            if (lane == leader) got = w;
           }
+          const int sdeg = deg < kWarpRow ? deg : 0;
+          const int incl = warp_incl_scan(sdeg);
+          const int total = __shfl_sync(kFull, incl, 31);
+          s_excl[wib][lane] = incl - sdeg;
+          s_rs[wib][lane] = rs;
+          s_w[wib][lane] = 0ull;
+          __syncwarp();
+          for (int e0 = 0; e0 < total; e0 += 64) {
+            const int ea = e0 + lane, eb = ea + 32;
+            int lo = 0, hi = 31, lo2 = 0, hi2 = 31;
+#pragma unroll
+            for (int it = 0; it < 5; it++) {
+              const int mid = (lo + hi + 1) >> 1, mid2 = (lo2 + hi2 + 1) >> 1;
+              if (s_excl[wib][mid] <= ea) lo = mid; else hi = mid - 1;
+              if (s_excl[wib][mid2] <= eb) lo2 = mid2; else hi2 = mid2 - 1;
+            }
+            const int32_t ca = ea < total ? __ldg(t_col + s_rs[wib][lo] + (ea - s_excl[wib][lo])) : -1;
+            const int32_t cb = eb < total ? __ldg(t_col + s_rs[wib][lo2] + (eb - s_excl[wib][lo2])) : -1;
+            u64 xa = ca >= 0 ? cur[ca - v0] : 0ull;
+            u64 xb = cb >= 0 ? cur[cb - v0] : 0ull;
+            // Lanes holding edges of one row are adjacent: OR them with a
+            // segmented warp scan, then the last lane of each row adds the
+            // row's bits to its slot (no two lanes write one slot at once).
+            const int ka = ea < total ? lo : 32, kb = eb < total ? lo2 : 32;
+            xa = seg_or_scan(xa, ka);
+            xb = seg_or_scan(xb, kb);
+            const int na = __shfl_down_sync(kFull, ka, 1), nb2 = __shfl_down_sync(kFull, kb, 1);
+            if (ka < 32 && (lane == 31 || na != ka) && xa) s_w[wib][ka] |= xa;
+            __syncwarp();
+            if (kb < 32 && (lane == 31 || nb2 != kb) && xb) s_w[wib][kb] |= xb;
+            __syncwarp();
+          }
+          __syncwarp();
+          if (sdeg > 0) got = s_w[wib][lane];
+          __syncwarp();
           nw = got & ~vis;
         }
+        if (!in) continue;
         nxt[u] = nw;
         if (nw) {
           visit[u] = vis | nw;
@@ -236,6 +372,13 @@ __global__ void __launch_bounds__(kPartBlock, 2) parts_traverse(PartsCtl* __rest
       }
     }
     __syncthreads();  // the slot is clean before the next task seeds it
+    if (tid == 0 && ctl->task_log) {
+      unsigned long long* r = ctl->task_log + 4 * (size_t)t;
+      r[0] = t_start;
+      r[1] = global_ns();
+      r[2] = ((unsigned long long)L << 32) | (unsigned)(t_push - push0);
+      r[3] = sm_id();
+    }
   }
   my_reached = warp_sum(my_reached);
   if (lane_id() == 0 && my_reached) atomicAdd(&ctl->reached, my_reached);
@@ -458,6 +601,11 @@ dawn_status parts_bfs(dawn_graph* g, const int32_t* source_offset, const int32_t
   c.tasks = g->pt_tasks.as<PartTask>();
   c.sources = g->pt_sources.as<int32_t>();
   c.dist = d_dist;
+  unsigned long long* d_log = nullptr;
+  if (g->trace) {
+    DAWN_CHECK(pool_alloc((void**)&d_log, sizeof(unsigned long long) * 4 * tasks.size(), g->stream));
+    c.task_log = d_log;
+  }
   DAWN_CUDA(cudaMemcpyAsync(g->pt_ctl.p, &c, sizeof(PartsCtl), cudaMemcpyHostToDevice, g->stream));
   DAWN_CUDA(cudaStreamSynchronize(g->stream));  // c lives on this stack frame
 
@@ -496,6 +644,30 @@ dawn_status parts_bfs(dawn_graph* g, const int32_t* source_offset, const int32_t
     parts_traverse<<<g->pt_slots, kPartBlock, 0, g->stream>>>(ctl, g->row_ptr, g->col, g->t_row_ptr, g->t_col, voff,
                                                          scratch, slot_words, maxn);
     DAWN_CUDA(cudaGetLastError());
+  }
+  if (d_log) {
+    // one trace record per task: device-clock start and duration
+    std::vector<unsigned long long> h(4 * tasks.size());
+    DAWN_CUDA(cudaMemcpyAsync(h.data(), d_log, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost,
+                              g->stream));
+    pool_free(d_log, g->stream);
+    DAWN_CUDA(cudaStreamSynchronize(g->stream));
+    unsigned long long t0 = ~0ull;
+    for (size_t i = 0; i < tasks.size(); i++) t0 = std::min(t0, h[4 * i]);
+    for (size_t i = 0; i < tasks.size(); i++) {
+      dawn_trace_rec r = {};
+      std::snprintf(r.kernel, sizeof(r.kernel), "parts_task");
+      const int p = tasks[i].part;
+      r.run = p;
+      r.level = (int32_t)(h[4 * i + 2] >> 32);
+      r.mode = (int32_t)(h[4 * i + 2] & 0xffffffffu);
+      r.pad = (int32_t)h[4 * i + 3];
+      r.frontier = tasks[i].nsrc;
+      r.frontier_edges = g->pt_pos[p + 1] - g->pt_pos[p];
+      r.unvisited_edges = (int64_t)(h[4 * i] - t0);
+      r.ms = (float)((double)(h[4 * i + 1] - h[4 * i]) * 1e-6);
+      g->trace_log.push_back(r);
+    }
   }
   if (st) {
     PartsCtl h;

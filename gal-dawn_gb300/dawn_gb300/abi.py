@@ -254,7 +254,7 @@ class Graph:
             for r in buf[:cnt.value]:
                 out.append({"kernel": r.kernel.decode(), "run": r.run, "level": r.level, "mode": r.mode,
                             "frontier": r.frontier, "frontier_edges": r.frontier_edges,
-                            "unvisited_edges": r.unvisited_edges, "ms": r.ms})
+                            "unvisited_edges": r.unvisited_edges, "ms": r.ms, "pad": r.pad})
             if cnt.value < 4096:
                 return out
 

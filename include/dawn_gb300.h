@@ -221,7 +221,12 @@ dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option,
  * uses, brackets each with CUDA events on the handle's stream, and appends
  * one record per kernel.  Results are identical; only speed differs.  The
  * records are the per-iteration timing log the variant selector trains on
- * and the per-kernel durations the roofline report divides by. */
+ * and the per-kernel durations the roofline report divides by.
+ * dawn_multi_* calls on a tracing handle run as usual and add one record
+ * per (part, source batch) task, kernel "parts_task": run = part, level =
+ * levels, mode = push levels, pad = SM, frontier = sources, frontier_edges
+ * = the part's edges, unvisited_edges = task start in ns after the first
+ * task's start, ms = task duration (device clock). */
 typedef struct dawn_trace_rec {
   char kernel[24];          /* kernel name */
   int32_t run;              /* source index (single-source) or batch index */
