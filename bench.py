@@ -132,11 +132,15 @@ def time_steps(torch, fn, steps, warmup, barrier):
     return e0.elapsed_time(e1)
 
 
+def HEADLINE_VARIANT(abi):
+    return abi.VARIANT_LEARNED
+
+
 def bitset_roofline(dg, g, srcs, d_dist, abi, peak_gbs, peak_kind):
     """Traced replay of one step: per-kernel CUDA-event durations, and the
     algorithmic bytes of each launch of the dominant kernel."""
     dg.trace(True)
-    dg.bfs_device(srcs, d_dist, variant=abi.VARIANT_BITSET, stats=False)
+    dg.bfs_device(srcs, d_dist, variant=HEADLINE_VARIANT(abi), stats=False)
     dg.synchronize()
     recs = dg.trace_read()
     dg.trace(False)
@@ -375,7 +379,7 @@ def main():
                     help="only the device-resident timing (profiling runs); prints a short JSON line")
     ap.add_argument("--traced", action="store_true",
                     help="with --quick: run the steps level by level, launching only the kernels each level uses")
-    ap.add_argument("--variant", default="bitset", choices=["bitset", "do", "push"])
+    ap.add_argument("--variant", default="bitset", choices=["bitset", "learned", "do", "push"])
     ap.add_argument("--suite", action="store_true",
                     help="also time the other workload shapes (one JSON line each, before the main line)")
     args = ap.parse_args()
@@ -408,7 +412,8 @@ def main():
     dg = abi.Graph(g, stream=stream)
     d_dist = torch.empty((NSRC, g.n), dtype=torch.int32, device="cuda")
     if args.quick:
-        var = {"bitset": abi.VARIANT_BITSET, "do": abi.VARIANT_DO, "push": abi.VARIANT_PUSH}[args.variant]
+        var = {"bitset": abi.VARIANT_BITSET, "learned": abi.VARIANT_LEARNED, "do": abi.VARIANT_DO,
+               "push": abi.VARIANT_PUSH}[args.variant]
         dg.trace(args.traced)
         quick = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=False)  # noqa: E731
         ms = time_steps(torch, quick, args.steps, args.warmup, barrier) / max(1, args.steps)
@@ -421,8 +426,11 @@ def main():
                               "kernels": len(recs)}), flush=True)
         dg.close()
         return
-    step = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=False)  # noqa
-    st = dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=True)
+    # learned + batched: the bitset traversal with each level's variant picked
+    # by the trained selector (the library's default weights)
+    var = HEADLINE_VARIANT(abi)
+    step = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=False)  # noqa
+    st = dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=True)
     edges = st.edges_traversed
 
     clocks = Clocks(local)
@@ -442,6 +450,14 @@ def main():
     ms_plain = time_steps(torch, step_plain, args.plain_steps, 1, barrier) / args.plain_steps
     plain = {"value": round(edges / (ms_plain * 1e-3) / 1e9, 3), "unit": "GTEPS",
              "ms_per_step": round(ms_plain, 3), "variant": "single-source push/pull (direction-optimising)"}
+    # the same batched traversal under the direction heuristic alone
+    step_h = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=False)  # noqa
+    ms_h = time_steps(torch, step_h, args.steps, args.warmup, barrier) / args.steps
+    st_h = dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=True)
+    batched_heuristic = {"value": round(edges / (ms_h * 1e-3) / 1e9, 3), "unit": "GTEPS",
+                         "ms_per_step": round(ms_h, 4), "push_levels": st_h.push_levels,
+                         "pull_levels": st_h.pull_levels,
+                         "variant": "batched bitset, direction heuristic (no selector)"}
 
     if os.environ.get("DAWN_BENCH_TRACE_PLAIN"):
         dg.trace(True)
@@ -469,7 +485,7 @@ def main():
         h = abi.Graph(raw=dict(n=g.n, m=g.m, row_ptr=rp_h.data_ptr(), col=col_h.data_ptr(), symmetric=True,
                                stream=stream))
         t1 = time.perf_counter()
-        h.bfs_host_ptr(srcs, out_h.data_ptr(), variant=abi.VARIANT_BITSET)
+        h.bfs_host_ptr(srcs, out_h.data_ptr(), variant=var)
         t2 = time.perf_counter()
         h.close()
         t3 = time.perf_counter()
@@ -500,12 +516,13 @@ def main():
     line = {"metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
-            "config": {"workload": f"rmat{args.scale}-ef{EDGEFACTOR}-bfs-{NSRC}src-bitset", "n": g.n, "m": g.m,
+            "config": {"workload": f"rmat{args.scale}-ef{EDGEFACTOR}-bfs-{NSRC}src-learned-bitset", "n": g.n,
+                       "m": g.m,
                        "sources": NSRC, "edges_traversed_per_step": edges,
                        "l2": "inputs larger than L2 (CSR %.0f MB, distances %.0f MB per step)" % (
                            (4 * g.m + 4 * g.n) / 2 ** 20, 4 * NSRC * g.n / 2 ** 20),
                        "parallelism": f"sources sharded, {ws} replica(s)"},
-            "clocks": clk, "e2e": e2e, "plain": plain,
+            "clocks": clk, "e2e": e2e, "plain": plain, "batched_heuristic": batched_heuristic,
             "speedup_vs_plain": round(value / plain["value"], 3) if plain["value"] else None,
             "roofline": roof, "cpu_baseline": cpu, "gpu_launches": launches * args.steps,
             "levels_per_step": st.levels, "push_levels": st.push_levels, "pull_levels": st.pull_levels}

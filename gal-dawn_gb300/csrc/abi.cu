@@ -4,10 +4,12 @@
 // live here; the traversals themselves are in bovm.cu (single-source
 // expand), msbfs.cu (64-source bitset expand) and govm.cu (min-plus relax).
 #include <climits>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "dawn_internal.cuh"
+#include "selector_default.inc"
 
 using dawn::DevBuf;
 
@@ -37,6 +39,7 @@ dawn_status finish_graph(dawn_graph* g, uint32_t flags) {
     DAWN_CHECK(dawn::build_transpose(g));
   }
   DAWN_CUDA(cudaMallocHost(&g->h_ctl, 2 * sizeof(dawn::SsCtl)));
+  DAWN_CHECK(dawn::ensure(g->sel_slot, sizeof(float) * DAWN_SELECTOR_WEIGHTS, g->stream));
   DAWN_CUDA(cudaEventCreate(&g->ev0));
   DAWN_CUDA(cudaEventCreate(&g->ev1));
   DAWN_CUDA(cudaStreamSynchronize(g->stream));
@@ -89,7 +92,8 @@ void destroy(dawn_graph* g) {
   if (g->val) dawn::pool_free(g->val, g->stream);
   DevBuf* bufs[] = {&g->ss_queues, &g->ss_segs, &g->bs_segs, &g->ss_bitmaps, &g->ss_ctl, &g->ss_sources, &g->ss_scratch,
                     &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
-                    &g->dist_stage, &g->pt_voff, &g->pt_tasks, &g->pt_sources, &g->pt_ctl, &g->pt_scratch, &g->pt_rows};
+                    &g->dist_stage, &g->pt_voff, &g->pt_tasks, &g->pt_sources, &g->pt_ctl, &g->pt_scratch, &g->pt_rows,
+                    &g->sel_slot};
   for (DevBuf* b : bufs) dawn::release(*b);
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
@@ -111,9 +115,40 @@ int32_t resolve_variant(int32_t variant, int32_t nsrc) {
   return variant;
 }
 
+// Whether this call's decide kernels evaluate the selector, and with which
+// weights in the handle's slot: the handle's own (dawn_graph_set_selector),
+// else for DAWN_VARIANT_LEARNED the library's trained defaults, else none
+// (direction heuristics).
+dawn_status call_selector(dawn_graph* g, int32_t variant, int32_t* use) {
+  *use = 0;
+  int want = g->sel_on ? 1 : 0;
+#if DAWN_HAVE_DEFAULT_SELECTOR
+  static_assert(sizeof(kDefaultSelectorWeights) == sizeof(float) * DAWN_SELECTOR_WEIGHTS,
+                "default selector weight count");
+  if (!want && variant == DAWN_VARIANT_LEARNED) want = 2;
+#else
+  (void)variant;
+#endif
+  if (!want) return DAWN_OK;
+  if (g->sel_slot_state != want) {
+#if DAWN_HAVE_DEFAULT_SELECTOR
+    const float* src = want == 1 ? g->sel_user.data() : kDefaultSelectorWeights;
+#else
+    const float* src = g->sel_user.data();
+#endif
+    DAWN_CUDA(cudaMemcpyAsync(g->sel_slot.p, src, sizeof(float) * DAWN_SELECTOR_WEIGHTS, cudaMemcpyHostToDevice,
+                              g->stream));
+    DAWN_CUDA(cudaStreamSynchronize(g->stream));
+    g->sel_slot_state = want;
+  }
+  *use = 1;
+  return DAWN_OK;
+}
+
 dawn_status bfs_device_impl(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,
                             int32_t variant, dawn_stats* st) {
   variant = resolve_variant(variant, nsrc);
+  DAWN_CHECK(call_selector(g, variant, &g->sel_call));
   if (st) {
     std::memset(st, 0, sizeof(*st));
     DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
@@ -626,10 +661,49 @@ dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value) 
       }
       g->bs_push_ratio = (int32_t)value;
       return DAWN_OK;
+    case DAWN_OPT_FORCE_VARIANT:
+      if (value < 0 || value > 3) {
+        dawn::set_error("forced variant must be 0 (decide per level), 1, 2 or 3");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      g->force_variant = (int32_t)value;
+      return DAWN_OK;
+    case DAWN_OPT_SELECTOR_MARGIN:
+      if (value < 0 || value > 100000) {
+        dawn::set_error("selector margin must lie in [0, 100000] thousandths");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      g->sel_margin = (float)value / 1000.0f;
+      return DAWN_OK;
     default:
       dawn::set_error("unknown option %d", option);
       return DAWN_ERR_INVALID_ARG;
   }
+}
+
+dawn_status dawn_graph_set_selector(dawn_graph* g, const float* weights, int32_t count) {
+  dawn::clear_error();
+  if (!g) {
+    dawn::set_error("graph is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  if (!weights) {
+    g->sel_on = false;
+    return DAWN_OK;
+  }
+  if (count != DAWN_SELECTOR_WEIGHTS) {
+    dawn::set_error("selector needs %d weights, got %d", DAWN_SELECTOR_WEIGHTS, count);
+    return DAWN_ERR_INVALID_ARG;
+  }
+  for (int32_t i = 0; i < count; i++)
+    if (!std::isfinite(weights[i])) {
+      dawn::set_error("selector weight %d is not finite", i);
+      return DAWN_ERR_INVALID_ARG;
+    }
+  g->sel_user.assign(weights, weights + count);
+  g->sel_on = true;
+  if (g->sel_slot_state == 1) g->sel_slot_state = 0;  // reload on the next call
+  return DAWN_OK;
 }
 
 dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option, int64_t* value) {
@@ -644,6 +718,12 @@ dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option, int64_t* 
       return DAWN_OK;
     case DAWN_OPT_PUSH_RATIO:
       *value = g->bs_push_ratio;
+      return DAWN_OK;
+    case DAWN_OPT_FORCE_VARIANT:
+      *value = g->force_variant;
+      return DAWN_OK;
+    case DAWN_OPT_SELECTOR_MARGIN:
+      *value = (int64_t)(g->sel_margin * 1000.0f + 0.5f);
       return DAWN_OK;
     default:
       dawn::set_error("unknown option %d", option);

@@ -18,6 +18,7 @@
 #include <mutex>
 
 #include "dawn_device.cuh"
+#include "selector.cuh"
 
 namespace dawn {
 namespace {
@@ -48,6 +49,9 @@ __global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ ro
   ctl->source = s;
   dist[s] = 0;
   vbm[s >> 5] |= 1u << (s & 31);
+  // level-0 frontier bitmap (the first of the three rotating ones, right
+  // after the visited words): read when the first level is a pull
+  vbm[(n + 31) / 32 + (s >> 5)] |= 1u << (s & 31);
   if (deg >= kLongRow) {
     const int nseg = (deg + kSeg - 1) / kSeg;
     for (int j = 0; j < nseg; j++) segs[j] = Seg{s, row_ptr[s] + j * kSeg};
@@ -65,7 +69,7 @@ __global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ ro
   ctl->mu = m - deg;
   ctl->reached = (unsigned long long)deg;
   ctl->level = 1;
-  ctl->mode = kModePush;
+  ctl->mode = ctl->force - 1 == kVarPull ? kModePull : kModePush;
   ctl->done = deg == 0;
   ctl->prev_nf = 1;
   ctl->n_push = 0;
@@ -183,38 +187,65 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }
 
-__global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop,
-                           int in_graph) {
-  if (threadIdx.x != 0) return;
-  if (ctl->done) {
-    if (in_graph) cudaGraphSetConditional(loop, 0);
-    return;
-  }
+// One warp.  Ends the loop when the frontier is empty, otherwise picks the
+// next level's direction: the forced variant if one is set, else the
+// learned selector if weights are loaded (direction-optimising calls only),
+// else Beamer's alpha/beta rule.
+__global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, const float* __restrict__ sel_w,
+                           cudaGraphConditionalHandle loop, int in_graph) {
+  const int lane = threadIdx.x;
+  if (sel_w) sel_prefetch(sel_w);
+  // every lane reads the control block before lane 0 changes it
+  const int done = ctl->done;
   const int L = ctl->level, pout = L & 1;
   const int nf = ctl->qsize[pout] + long_vertices(ctl->lpack[pout]);
   const unsigned long long mf = ctl->mf[pout];
-  ctl->reached += mf;
-  ctl->mu -= (long long)mf;
-  if (ctl->mode == kModePush) ctl->n_push++; else ctl->n_pull++;
-  if (nf == 0 || L >= n) {
-    ctl->done = 1;
-    if (in_graph) cudaGraphSetConditional(loop, 0);
+  const long long mu = ctl->mu - (long long)mf;
+  const int cur_mode = ctl->mode, prev_nf = ctl->prev_nf, policy = ctl->policy, force = ctl->force;
+  const bool sel = ctl->use_sel && sel_w;
+  const long long m = ctl->m;
+  __syncwarp();
+  if (done) {
+    if (lane == 0 && in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
-  ctl->qsize[pout ^ 1] = 0;
-  ctl->lpack[pout ^ 1] = 0;
-  ctl->mf[pout ^ 1] = 0;
-  int mode = ctl->mode;
-  if (ctl->policy == DAWN_VARIANT_DO) {
+  if (lane == 0) {
+    ctl->reached += mf;
+    ctl->mu = mu;
+    if (cur_mode == kModePush) ctl->n_push++; else ctl->n_pull++;
+  }
+  if (nf == 0 || L >= n) {
+    if (lane == 0) {
+      ctl->done = 1;
+      if (in_graph) cudaGraphSetConditional(loop, 0);
+    }
+    return;
+  }
+  int mode = cur_mode;
+  if (policy == DAWN_VARIANT_DO) {
     if (mode == kModePush) {
-      if ((long long)mf * kAlpha > ctl->mu && nf > ctl->prev_nf) mode = kModePull;
+      if ((long long)mf * kAlpha > mu && nf > prev_nf) mode = kModePull;
     } else {
-      if ((long long)nf * kBeta < (long long)n && nf < ctl->prev_nf) mode = kModePush;
+      if ((long long)nf * kBeta < (long long)n && nf < prev_nf) mode = kModePush;
     }
   }
-  ctl->prev_nf = nf;
-  ctl->mode = mode;
-  ctl->level = L + 1;
+  if (force) {
+    mode = force - 1 == kVarPull ? kModePull : kModePush;
+  } else if (policy == DAWN_VARIANT_DO && sel) {
+    float x[kSelIn];
+    sel_features(x, (float)n, (float)m, (float)nf, (float)mf, (float)mu, (float)(L + 1), (float)prev_nf, 1.0f);
+    const int h = mode == kModePull ? kVarPull : kVarPush;
+    mode = sel_pick(sel_w, x, (1u << kVarPush) | (1u << kVarPull), h, ctl->sel_margin) == kVarPull ? kModePull
+                                                                                                : kModePush;
+  }
+  if (lane == 0) {
+    ctl->qsize[pout ^ 1] = 0;
+    ctl->lpack[pout ^ 1] = 0;
+    ctl->mf[pout ^ 1] = 0;
+    ctl->prev_nf = nf;
+    ctl->mode = mode;
+    ctl->level = L + 1;
+  }
 }
 
 __global__ void ss_next(SsCtl* __restrict__ ctl) {
@@ -257,6 +288,10 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   c.nsrc = nsrc;
   c.dist_base = d_dist;
   c.sources = g->ss_sources.as<int32_t>();
+  c.use_sel = g->sel_call;
+  c.sel_margin = g->sel_margin;
+  c.force = g->force_variant == 3 ? 1 + kVarPush : g->force_variant;
+  c.m = m;
   DAWN_CHECK(upload_ctl(g, c));
 
   struct {
@@ -270,7 +305,9 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
     long long m;
     cudaGraphConditionalHandle handle;
     int in_graph;
+    const float* sel_w;
   } a;
+  a.sel_w = g->sel_slot.as<float>();
   a.ctl = g->ss_ctl.as<SsCtl>();
   a.row_ptr = g->row_ptr;
   a.col = g->col;
@@ -292,7 +329,7 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   void* push_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm, &a.n, &a.nwords};
   void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm,
                        &a.n, &a.nwords};
-  void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
+  void* decide_args[] = {&a.ctl, &a.n, &a.sel_w, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
 
   const int sms = g->geo.sms;
@@ -499,7 +536,7 @@ dawn_status bfs_static(const int32_t* row_ptr, const int32_t* col, int32_t n, in
     for (int j = 0; j < kStaticPollLevels; j++) {
       bfs_push<<<d.push_blocks, kBlock, 0, stream>>>(row_ptr, col, ctl, q, segs, kStaticSegCap, vbm, fbm, n,
                                                       nwords);
-      bfs_decide<<<1, 32, 0, stream>>>(ctl, n, 0, 0);
+      bfs_decide<<<1, 32, 0, stream>>>(ctl, n, nullptr, 0, 0);
     }
     DAWN_CUDA(cudaGetLastError());
     int32_t done = 0;

@@ -79,6 +79,11 @@ struct SsCtl {
   // per-call parameters (host-written before the first launch)
   int32_t* dist_base;           // nsrc x n output, row src_idx is current
   const int32_t* sources;       // device copy of the source list
+  int32_t use_sel;              // decide with the handle's selector weights
+  int32_t force;                // 0 = decide per level; 1 + variant = always that variant
+  float sel_margin;             // log2 margin by which the selector must beat the heuristic
+  int32_t pad4;
+  long long m;                  // CSR entries (selector input)
   // accumulated over all sources of the call
   unsigned long long total_reached;
   int32_t total_levels, total_push, total_pull, pad2;
@@ -188,6 +193,16 @@ struct dawn_graph {
   int32_t hv_count = 0, hv_segs = 0;
   int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges
   int32_t bs_width = 0;         // words per vertex of the bitset traversal (0 = by source count)
+  int32_t force_variant = 0;    // 0 = decide per level, else 1 + variant for every level
+  // Learned selector.  The decide kernels take the slot's address as a
+  // launch argument (fixed for the handle's life, so captured graphs stay
+  // valid) and prefetch it while they read the control block.
+  dawn::DevBuf sel_slot;        // weights the next call evaluates
+  int32_t sel_slot_state = 0;   // 0 nothing loaded, 1 the handle's own, 2 the library's defaults
+  std::vector<float> sel_user;  // dawn_graph_set_selector weights (host copy)
+  bool sel_on = false;
+  int32_t sel_call = 0;         // the running call uses the slot
+  float sel_margin = 0.0f;      // DAWN_OPT_SELECTOR_MARGIN / 1000
 
   // disjoint-union parts (dawn_graph_set_parts)
   std::vector<int32_t> pt_off;   // nparts + 1 vertex offsets (empty: no parts)

@@ -27,6 +27,7 @@
 // them into the distance block with full-line coalesced stores, writing -1
 // for pairs never reached.
 #include "dawn_device.cuh"
+#include "selector.cuh"
 
 namespace dawn {
 namespace {
@@ -55,6 +56,12 @@ struct BsCtl {
   unsigned long long full[kMaxW];  // this batch's source bits
   int32_t* dist_base;
   const int32_t* sources;
+  int32_t use_sel;              // decide with the handle's selector weights
+  float sel_margin;             // log2 margin by which the selector must beat the heuristic
+  int32_t force;                // 0 = decide per level; 1 + variant = always that variant
+  int32_t prev_nf;              // frontier size entering the current level
+  int32_t pad3;
+  long long m;                  // CSR entries (selector input)
   unsigned long long total_reached;
   int32_t total_levels, total_push, total_pull, pad2;
 };
@@ -297,7 +304,9 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     ctl->mu = m - (long long)s_dec;
     ctl->mu_dec = 0;
     ctl->level = 1;
-    ctl->mode = kModePush;
+    ctl->mode = ctl->force - 1 == kVarPull ? kModePull : kModePush;
+    ctl->dense = ctl->force - 1 == kVarDense;
+    ctl->prev_nf = 0;
     ctl->done = 0;
     ctl->n_push = 0;
     ctl->n_pull = 0;
@@ -696,45 +705,81 @@ __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__
   }
 }
 
-__global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop, int in_graph) {
-  if (threadIdx.x != 0) return;
-  if (ctl->done) {
-    if (in_graph) cudaGraphSetConditional(loop, 0);
-    return;
-  }
+// One warp.  Ends the batch when the frontier is empty, otherwise picks
+// the next level's variant: the forced one if set, else the learned
+// selector if weights are loaded, else push while
+// push_ratio x frontier edges < unfinished in-edges, dense once the
+// frontier's edges reach n / 16.
+__global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, const float* __restrict__ sel_w,
+                          cudaGraphConditionalHandle loop, int in_graph) {
+  const int lane = threadIdx.x;
+  if (sel_w) sel_prefetch(sel_w);
+  // every lane reads the control block before lane 0 changes it
+  const int done = ctl->done;
   const int L = ctl->level;
-  if (ctl->mode == kModePush) {
-    ctl->n_push++;
-  } else {
-    ctl->n_pull++;
-    ctl->ul_cur = ctl->ul_cur < 0 ? 0 : ctl->ul_cur ^ 1;
-    ctl->ul_size[ctl->ul_cur ^ 1] = 0;
-  }
-  ctl->mu -= ctl->mu_dec;
-  ctl->mu_dec = 0;
-  ctl->tq_size = 0;
-  ctl->work = 0;
-  ctl->hwork = 0;
+  const int cur_mode = ctl->mode, ul_cur = ctl->ul_cur;
+  const long long mu = ctl->mu - ctl->mu_dec;
   const int nf = ctl->aq_size[L % 3] + long_vertices(ctl->alpack[L % 3]);
-  if (nf == 0 || L >= n) {
-    ctl->done = 1;
-    if (in_graph) cudaGraphSetConditional(loop, 0);
+  const long long mf = (long long)ctl->mf[L % 3];
+  const int policy = ctl->policy, ratio = ctl->push_ratio, force = ctl->force, prev_nf = ctl->prev_nf;
+  const bool sel = ctl->use_sel && sel_w;
+  const float sel_margin = ctl->sel_margin;
+  const long long m = ctl->m;
+  const int per = 64 * ctl->width;
+  const int nb = min(per, ctl->nsrc - ctl->batch * per);
+  __syncwarp();
+  if (done) {
+    if (lane == 0 && in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
-  // Level L+1 writes list (L+1)%3, whose stale frontier words level L cleared.
-  ctl->aq_size[(L + 1) % 3] = 0;
-  ctl->alpack[(L + 1) % 3] = 0;
-  ctl->mf[(L + 1) % 3] = 0;
-  int mode;
-  if (ctl->policy == DAWN_VARIANT_PUSH)
-    mode = kModePush;
-  else
-    mode = (long long)ctl->mf[L % 3] * ctl->push_ratio < ctl->mu ? kModePush : kModePull;
-  // A push whose frontier edges reach n/16 touches enough vertices that a
-  // dense update sweep beats queueing every first touch.
-  ctl->dense = (long long)ctl->mf[L % 3] * 16 >= (long long)n;
-  ctl->mode = mode;
-  ctl->level = L + 1;
+  if (lane == 0) {
+    if (cur_mode == kModePush) {
+      ctl->n_push++;
+    } else {
+      ctl->n_pull++;
+      ctl->ul_cur = ul_cur < 0 ? 0 : ul_cur ^ 1;
+      ctl->ul_size[(ul_cur < 0 ? 0 : ul_cur ^ 1) ^ 1] = 0;
+    }
+    ctl->mu = mu;
+    ctl->mu_dec = 0;
+    ctl->tq_size = 0;
+    ctl->work = 0;
+    ctl->hwork = 0;
+  }
+  if (nf == 0 || L >= n) {
+    if (lane == 0) {
+      ctl->done = 1;
+      if (in_graph) cudaGraphSetConditional(loop, 0);
+    }
+    return;
+  }
+  int variant;
+  if (policy == DAWN_VARIANT_PUSH || mf * ratio < mu) {
+    // A push whose frontier edges reach n/16 touches enough vertices that a
+    // dense update sweep beats queueing every first touch.
+    variant = mf * 16 >= (long long)n ? kVarDense : kVarPush;
+  } else {
+    variant = kVarPull;
+  }
+  if (force) {
+    variant = force - 1;
+  } else if (sel) {
+    float x[kSelIn];
+    sel_features(x, (float)n, (float)m, (float)nf, (float)mf, (float)mu, (float)(L + 1), (float)prev_nf,
+                 (float)nb);
+    const unsigned allowed = policy == DAWN_VARIANT_PUSH ? (1u << kVarPush) | (1u << kVarDense) : 7u;
+    variant = sel_pick(sel_w, x, allowed, variant, sel_margin);
+  }
+  if (lane == 0) {
+    // Level L+1 writes list (L+1)%3, whose stale frontier words level L cleared.
+    ctl->aq_size[(L + 1) % 3] = 0;
+    ctl->alpack[(L + 1) % 3] = 0;
+    ctl->mf[(L + 1) % 3] = 0;
+    ctl->dense = variant == kVarDense;
+    ctl->mode = variant == kVarPull ? kModePull : kModePush;
+    ctl->prev_nf = nf;
+    ctl->level = L + 1;
+  }
 }
 
 __global__ void bs_next(BsCtl* __restrict__ ctl) {
@@ -862,6 +907,10 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   c.width = W;
   c.dist_base = d_dist;
   c.sources = g->bs_sources.as<int32_t>();
+  c.use_sel = g->sel_call;
+  c.sel_margin = g->sel_margin;
+  c.force = g->force_variant;
+  c.m = g->m;
   DAWN_CUDA(cudaMemcpyAsync(g->bs_ctl.p, &c, sizeof(BsCtl), cudaMemcpyHostToDevice, g->stream));
 
   struct {
@@ -880,7 +929,9 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
     long long m;
     cudaGraphConditionalHandle handle;
     int in_graph;
+    const float* sel_w;
   } a;
+  a.sel_w = g->sel_slot.as<float>();
   a.ctl = g->bs_ctl.as<BsCtl>();
   a.row_ptr = g->row_ptr;
   a.col = g->col;
@@ -921,7 +972,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
                          &a.segcap, &a.tq, &a.tbm, &a.n};
   void* emit_args[] = {&a.ctl, &a.visit, &a.slices, &a.n};
-  void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
+  void* decide_args[] = {&a.ctl, &a.n, &a.sel_w, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
   const int sms = g->geo.sms;
   SsFamily fam;

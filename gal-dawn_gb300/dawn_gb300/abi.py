@@ -24,9 +24,10 @@ LIB_PATH = os.path.join(LIB_DIR, "libdawn_gb300.so")
 EXPORTS = ("dawn_graph_create", "dawn_graph_create_device", "dawn_graph_destroy",
            "dawn_graph_set_stream", "dawn_graph_synchronize", "dawn_bfs", "dawn_bfs_device", "dawn_bfs_static",
            "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_graph_set_option",
-           "dawn_graph_get_option", "dawn_graph_set_parts", "dawn_multi_bfs", "dawn_multi_bfs_device",
+           "dawn_graph_get_option", "dawn_graph_set_selector", "dawn_graph_set_parts", "dawn_multi_bfs", "dawn_multi_bfs_device",
            "dawn_multi_closeness", "dawn_trace_enable", "dawn_trace_read", "dawn_last_error", "dawn_version")
-OPT_BITSET_WIDTH, OPT_PUSH_RATIO = 1, 2
+OPT_BITSET_WIDTH, OPT_PUSH_RATIO, OPT_FORCE_VARIANT, OPT_SELECTOR_MARGIN = 1, 2, 3, 4
+SELECTOR_WEIGHTS = 1475
 
 
 class DawnError(RuntimeError):
@@ -81,6 +82,7 @@ def lib():
                                      ctypes.POINTER(Stats)]
         L.dawn_graph_set_option.argtypes = [_VP, ctypes.c_int32, ctypes.c_int64]
         L.dawn_graph_get_option.argtypes = [_VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
+        L.dawn_graph_set_selector.argtypes = [_VP, _VP, ctypes.c_int32]
         L.dawn_graph_set_parts.argtypes = [_VP, ctypes.c_int32, _VP]
         L.dawn_multi_bfs.argtypes = [_VP, _VP, _VP, _VP, ctypes.POINTER(Stats)]
         L.dawn_multi_bfs_device.argtypes = L.dawn_multi_bfs.argtypes
@@ -190,6 +192,21 @@ class Graph:
         v = ctypes.c_int64()
         _check(lib().dawn_graph_get_option(self.handle, option, ctypes.byref(v)))
         return v.value
+
+    def set_selector(self, weights):
+        """dawn_graph_set_selector: load MLP weights (1475 floats) or None."""
+        if weights is None:
+            _check(lib().dawn_graph_set_selector(self.handle, None, 0))
+            return
+        w = np.ascontiguousarray(weights, np.float32)
+        _check(lib().dawn_graph_set_selector(self.handle, _ptr(w), int(w.size)))
+
+    def bfs_stats(self, sources, variant=VARIANT_AUTO):
+        """dawn_bfs with dist = NULL: the traversal runs, only statistics return."""
+        s = np.ascontiguousarray(sources, np.int32)
+        st = Stats()
+        _check(lib().dawn_bfs(self.handle, _ptr(s), len(s), None, variant, ctypes.byref(st)))
+        return st
 
     def set_parts(self, offsets):
         """dawn_graph_set_parts: the graph is the disjoint union of the

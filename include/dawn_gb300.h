@@ -50,7 +50,9 @@ typedef enum dawn_wtype {
 #define DAWN_VARIANT_PUSH 1    /* single source, top-down queue every level */
 #define DAWN_VARIANT_DO 2      /* single source, push/pull by heuristic */
 #define DAWN_VARIANT_BITSET 3  /* batched: 64 sources per uint64 frontier word */
-#define DAWN_VARIANT_LEARNED 4 /* batched, per-level kernel chosen by the MLP */
+#define DAWN_VARIANT_LEARNED 4 /* batched; each level's variant picked by the learned
+                                  selector (dawn_graph_set_selector weights,
+                                  else the library's trained ones) */
 
 typedef struct dawn_stats {
   int64_t edges_traversed; /* TEPS numerator: sum over sources of the CSR
@@ -209,9 +211,36 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources,
  *                          edges of unfinished vertices (default 4) */
 #define DAWN_OPT_BITSET_WIDTH 1
 #define DAWN_OPT_PUSH_RATIO 2
+/*   DAWN_OPT_FORCE_VARIANT every level of BFS traversals runs one variant:
+ *                          0 = decide per level (default), 1 = sparse push,
+ *                          2 = bitmap pull, 3 = dense push (batched bitset
+ *                          only; single-source runs it as sparse push).
+ *                          For recording the per-variant level timings the
+ *                          selector is trained on; distances are unchanged. */
+#define DAWN_OPT_FORCE_VARIANT 3
+/*   DAWN_OPT_SELECTOR_MARGIN the learned selector overrides the direction
+ *                          heuristic only when it predicts the other variant
+ *                          faster by this many thousandths of a log2 unit
+ *                          (default 0: ties go to the heuristic; 250 asks
+ *                          for a predicted gain of about 19%). */
+#define DAWN_OPT_SELECTOR_MARGIN 4
 dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value);
 dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option,
                                   int64_t* value);
+
+/* Learned per-level variant selector (no counterpart in the reference).
+ * weights: DAWN_SELECTOR_WEIGHTS floats of a 9 x 32 x 32 x 3 ReLU MLP,
+ * row-major W1[32][9], b1[32], W2[32][32], b2[32], W3[3][32], b3[3], that
+ * predicts log2 of a level's duration in microseconds for sparse push,
+ * bitmap pull and dense push from nine frontier statistics.  The decide
+ * kernel of each level (one warp, on the device) runs the variant with the
+ * smallest prediction when it beats the direction heuristic's choice by
+ * DAWN_OPT_SELECTOR_MARGIN, else the heuristic's choice: the heuristic is
+ * both the fallback and the judge.  weights = NULL (count 0) restores the
+ * heuristics alone.  Distances never depend on the choice. */
+#define DAWN_SELECTOR_WEIGHTS 1475
+dawn_status dawn_graph_set_selector(dawn_graph* g, const float* weights,
+                                    int32_t count);
 
 /* Per-level trace.  No counterpart in the reference, which only times whole
  * runs with host std::chrono (src/algorithm/gpu/bfs.cu:70,93-95).  While

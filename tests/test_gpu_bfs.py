@@ -166,3 +166,46 @@ def test_width_changes_on_one_handle():
             dg.set_option(abi.OPT_BITSET_WIDTH, width)
             d, _ = dg.bfs(srcs[:k], variant=abi.VARIANT_BITSET)
             assert np.array_equal(d, want[:k]), (width, k)
+
+
+@pytest.mark.parametrize("force", [1, 2, 3])
+def test_forced_variants_change_nothing(force):
+    # every level forced to sparse push, bitmap pull or dense push (the
+    # per-variant timings the selector is trained on) gives the same distances
+    g = gen.rmat(14, 8, seed=41)
+    srcs = gen.sources(g, 70, seed=42)
+    want, edges = expected(g, srcs)
+    with abi.Graph(g) as dg:
+        dg.set_option(abi.OPT_FORCE_VARIANT, force)
+        for v, k in ((abi.VARIANT_BITSET, 70), (abi.VARIANT_DO, 3), (abi.VARIANT_PUSH, 2)):
+            d, st = dg.bfs(srcs[:k], variant=v)
+            assert np.array_equal(d, want[:k]), (force, v)
+            assert st.edges_traversed == (edges if k == 70 else st.edges_traversed)
+        d, _ = dg.bfs(srcs[:40], variant=abi.VARIANT_BITSET)
+        assert np.array_equal(d, want[:40])
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_random_selector_changes_nothing(seed):
+    # a selector with arbitrary weights makes arbitrary per-level choices;
+    # the distances stay those of the oracle
+    rng = np.random.default_rng(seed)
+    w = (rng.standard_normal(abi.SELECTOR_WEIGHTS) * 0.5).astype(np.float32)
+    g = gen.rmat(14, 8, seed=43)
+    srcs = gen.sources(g, 130, seed=44)
+    want, edges = expected(g, srcs)
+    grid = gen.grid(40, 60)
+    gs = np.array([0, 1234, 2399], np.int32)
+    gwant, _ = expected(grid, gs)
+    with abi.Graph(g) as dg, abi.Graph(grid) as dgrid:
+        for h in (dg, dgrid):
+            h.set_selector(w)
+        for v in (abi.VARIANT_BITSET, abi.VARIANT_LEARNED, abi.VARIANT_DO):
+            k = 130 if v != abi.VARIANT_DO else 4
+            d, st = dg.bfs(srcs[:k], variant=v)
+            assert np.array_equal(d, want[:k]), v
+            d, _ = dgrid.bfs(gs, variant=v)
+            assert np.array_equal(d, gwant), v
+        dg.set_selector(None)
+        d, _ = dg.bfs(srcs, variant=abi.VARIANT_BITSET)
+        assert np.array_equal(d, want)

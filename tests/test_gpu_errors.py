@@ -54,3 +54,21 @@ def test_bad_options_rejected():
             assert e.value.status == abi.ERR_INVALID_ARG
         assert dg.get_option(abi.OPT_BITSET_WIDTH) == 0
         assert dg.get_option(abi.OPT_PUSH_RATIO) == 4
+
+
+def test_bad_selector_rejected():
+    g = gen.rmat(8, 4, seed=3)
+    with abi.Graph(g) as dg:
+        with pytest.raises(abi.DawnError) as e:
+            dg.set_selector(np.zeros(100, np.float32))
+        assert e.value.status == abi.ERR_INVALID_ARG
+        w = np.zeros(abi.SELECTOR_WEIGHTS, np.float32)
+        w[7] = np.nan
+        with pytest.raises(abi.DawnError):
+            dg.set_selector(w)
+        for bad in (-1, 4):
+            with pytest.raises(abi.DawnError):
+                dg.set_option(abi.OPT_FORCE_VARIANT, bad)
+        dg.set_selector(None)
+        d, _ = dg.bfs([0], variant=abi.VARIANT_LEARNED)
+        assert d[0, 0] == 0
