@@ -333,6 +333,19 @@ def suite_lines(torch, abi, gen, stream, rank):
         st2 = dg.bfs_device(srcs[:256], d.data_ptr(), variant=abi.VARIANT_DO)
         out.append({"suite": "rmat18-bfs-4096src", "variant": "plain (first 256 sources)",
                     "ms_per_step": round(ms, 3), "gteps": round(st2.edges_traversed / (ms * 1e-3) / 1e9, 2)})
+        # closeness of the same 4,096 sources, reduced inside the traversal
+        _, _, _, st_cc = dg.closeness(srcs, with_stats=True)
+        out.append({"suite": "rmat18-closeness", "sources": 4096, "device_ms": round(st_cc.device_ms, 3),
+                    "gteps": round(st_cc.edges_traversed / (st_cc.device_ms * 1e-3) / 1e9, 2),
+                    "note": "no distance matrix: per-source sums from the level words"})
+        allv = np.arange(g.n, dtype=np.int32)
+        t0 = time.perf_counter()
+        _, _, _, st_all = dg.closeness(allv, with_stats=True)
+        wall = time.perf_counter() - t0
+        out.append({"suite": "rmat18-closeness", "sources": int(g.n), "device_ms": round(st_all.device_ms, 3),
+                    "wall_ms": round(wall * 1e3, 3),
+                    "gteps": round(st_all.edges_traversed / (st_all.device_ms * 1e-3) / 1e9, 2),
+                    "note": "all-vertex closeness (every vertex a source)"})
     del g, d
     # 512 independent directed ER graphs, 8-64 sources each, one persistent launch
     graphs, gsrcs = gen.er_family(ngraphs=512, seed=GRAPH_SEED)

@@ -492,6 +492,36 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, 
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (nsrc == 0) return DAWN_OK;
   const int kind = !weighted ? 0 : (g->wtype == DAWN_W_F32 ? 2 : 1);
+  if (kind == 0) {
+    // Hop closeness straight from the batched traversal's level words: its
+    // final pass sums each source's distances instead of writing them, so
+    // no distance matrix is formed.
+    DAWN_CHECK(dawn::ensure(g->cc_out, 2 * sizeof(unsigned long long) * (size_t)nsrc, g->stream));
+    unsigned long long* d_sum = g->cc_out.as<unsigned long long>();
+    unsigned long long* d_cnt = d_sum + nsrc;
+    DAWN_CUDA(cudaMemsetAsync(d_sum, 0, 2 * sizeof(unsigned long long) * (size_t)nsrc, g->stream));
+    DAWN_CHECK(call_selector(g, DAWN_VARIANT_BITSET, &g->sel_call));
+    if (stats) DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
+    DAWN_CHECK(dawn::bfs_bitset(g, sources, nsrc, nullptr, d_sum, d_cnt));
+    if (stats) {
+      DAWN_CUDA(cudaEventRecord(g->ev1, g->stream));
+      DAWN_CHECK(dawn::bfs_bitset_stats(g, stats, nsrc));
+      DAWN_CUDA(cudaEventSynchronize(g->ev1));
+      DAWN_CUDA(cudaEventElapsedTime(&stats->device_ms, g->ev0, g->ev1));
+    }
+    std::vector<unsigned long long> h(2 * (size_t)nsrc);
+    DAWN_CUDA(cudaMemcpyAsync(h.data(), d_sum, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost,
+                              g->stream));
+    DAWN_CUDA(cudaStreamSynchronize(g->stream));
+    for (int32_t i = 0; i < nsrc; i++) {
+      const double total = (double)h[i];
+      cc[i] = total > 0 ? (double)(g->n - 1) / total : 0.0;
+      if (dist_sum) dist_sum[i] = total;
+      // the count includes the source's own bit (level 0)
+      if (reached) reached[i] = (int64_t)h[nsrc + i] - 1;
+    }
+    return DAWN_OK;
+  }
   const size_t row_bytes = sizeof(int32_t) * (size_t)g->n;
   int32_t chunk = (int32_t)(kStageBytes / row_bytes);
   if (chunk >= 64) chunk -= chunk % 64;

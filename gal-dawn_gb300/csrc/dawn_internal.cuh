@@ -250,8 +250,12 @@ dawn_status bfs_static(const int32_t* row_ptr, const int32_t* col, int32_t n,
                        int64_t m, int32_t source, int32_t* dist, uint32_t flags,
                        cudaStream_t stream);
 // msbfs.cu
+// d_dist (nsrc x n) receives the distances; or, with cc_sum / cc_cnt set
+// (zeroed by the caller, nsrc entries each), each source's hop-distance sum
+// and reached count accumulate there and no distances are written.
 dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc,
-                       int32_t* d_dist);
+                       int32_t* d_dist, unsigned long long* cc_sum = nullptr,
+                       unsigned long long* cc_cnt = nullptr);
 dawn_status bfs_bitset_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc);
 int bitset_width(const dawn_graph* g, int32_t nsrc);
 // govm.cu

@@ -56,6 +56,8 @@ struct BsCtl {
   unsigned long long full[kMaxW];  // this batch's source bits
   int32_t* dist_base;
   const int32_t* sources;
+  unsigned long long* cc_sum;   // closeness mode: per source, sum of hop distances (else NULL)
+  unsigned long long* cc_cnt;   // closeness mode: per source, vertices reached besides itself
   int32_t use_sel;              // decide with the handle's selector weights
   float sel_margin;             // log2 margin by which the selector must beat the heuristic
   int32_t force;                // 0 = decide per level; 1 + variant = always that variant
@@ -682,9 +684,79 @@ __device__ __forceinline__ void emit_vertex(int32_t* __restrict__ dist, int32_t 
   }
 }
 
+// 32 x 32 bit transpose across a warp: lane i holds row i on entry and
+// column i on exit (bit j of lane i's result = bit i of lane j's input).
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+  const int lane = lane_id();
+  const uint32_t left[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int t = 0; t < 5; t++) {
+    const int s = 16 >> t;
+    const uint32_t y = __shfl_xor_sync(kFull, x, s);
+    x = (lane & s) ? ((x & ~left[t]) | ((y & ~left[t]) >> s)) : ((x & left[t]) | ((y & left[t]) << s));
+  }
+  return x;
+}
+
+// Closeness mode of the final pass: per source of the batch, the sum of its
+// hop distances (sum over level bits k of 2^k x the vertices whose slice k
+// holds the source's bit) and the vertices it reached besides itself,
+// without writing distances.  Each warp transposes the words of 32
+// consecutive vertices so lane j holds bit j (and j + 32) of all of them and
+// counts them with popc; CTA totals go to the batch's rows with one atomic
+// per source.
+template <int W>
+__device__ __forceinline__ void emit_closeness(const BsCtl* __restrict__ ctl, const u64* __restrict__ visit,
+                                               const u64* __restrict__ slices, int32_t n, int nb, int nbits) {
+  __shared__ unsigned long long s_sum[64 * W], s_cnt[64 * W];
+  for (int t = threadIdx.x; t < 64 * W; t += blockDim.x) {
+    s_sum[t] = 0;
+    s_cnt[t] = 0;
+  }
+  __syncthreads();
+  const int lane = lane_id();
+#pragma unroll
+  for (int i = 0; i < W; i++) {
+    if (64 * i >= nb) break;
+    unsigned long long sum_lo = 0, sum_hi = 0, cnt_lo = 0, cnt_hi = 0;
+    for (int base = global_warp() * 32; base < n; base += num_warps() * 32) {
+      const int u = base + lane;
+      const bool in = u < n;
+      const u64 vis = in ? visit[(size_t)u * W + i] : 0ull;
+      cnt_lo += __popc(warp_transpose32((uint32_t)vis));
+      cnt_hi += __popc(warp_transpose32((uint32_t)(vis >> 32)));
+      for (int k = 0; k < nbits; k++) {
+        const u64 x = in ? slices[((size_t)k * n + u) * W + i] : 0ull;
+        sum_lo += (unsigned long long)__popc(warp_transpose32((uint32_t)x)) << k;
+        sum_hi += (unsigned long long)__popc(warp_transpose32((uint32_t)(x >> 32))) << k;
+      }
+    }
+    if (cnt_lo | sum_lo) {
+      atomicAdd(&s_cnt[64 * i + lane], cnt_lo);
+      atomicAdd(&s_sum[64 * i + lane], sum_lo);
+    }
+    if (cnt_hi | sum_hi) {
+      atomicAdd(&s_cnt[64 * i + 32 + lane], cnt_hi);
+      atomicAdd(&s_sum[64 * i + 32 + lane], sum_hi);
+    }
+  }
+  __syncthreads();
+  const size_t row0 = (size_t)ctl->batch * 64 * W;
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    if (s_sum[t]) atomicAdd(ctl->cc_sum + row0 + t, s_sum[t]);
+    if (s_cnt[t]) atomicAdd(ctl->cc_cnt + row0 + t, s_cnt[t]);
+  }
+}
+
 template <int W>
 __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__ ctl, const u64* __restrict__ visit,
                                                        const u64* __restrict__ slices, int32_t n) {
+  if (ctl->cc_sum) {
+    const int per = 64 * W;
+    emit_closeness<W>(ctl, visit, slices, n, min(per, ctl->nsrc - ctl->batch * per),
+                      32 - __clz(max(ctl->level, 1)));
+    return;
+  }
   const int batch = ctl->batch;
   const int per = 64 * W;
   const int nb = min(per, ctl->nsrc - batch * per);
@@ -872,7 +944,8 @@ dawn_status build_static_list(dawn_graph* g) {
 }
 
 template <int W>
-dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist) {
+dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,
+                      unsigned long long* cc_sum, unsigned long long* cc_cnt) {
   const int32_t n = g->n;
   const size_t nn = (size_t)n;
   const int wi = W == 1 ? 0 : (W == 2 ? 1 : 2);
@@ -907,6 +980,8 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   c.width = W;
   c.dist_base = d_dist;
   c.sources = g->bs_sources.as<int32_t>();
+  c.cc_sum = cc_sum;
+  c.cc_cnt = cc_cnt;
   c.use_sel = g->sel_call;
   c.sel_margin = g->sel_margin;
   c.force = g->force_variant;
@@ -1011,11 +1086,12 @@ int bitset_width(const dawn_graph* g, int32_t nsrc) {
   return 1;
 }
 
-dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist) {
+dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,
+                       unsigned long long* cc_sum, unsigned long long* cc_cnt) {
   const int w = bitset_width(g, nsrc);
-  if (w == 4) return run_width<4>(g, sources, nsrc, d_dist);
-  if (w == 2) return run_width<2>(g, sources, nsrc, d_dist);
-  return run_width<1>(g, sources, nsrc, d_dist);
+  if (w == 4) return run_width<4>(g, sources, nsrc, d_dist, cc_sum, cc_cnt);
+  if (w == 2) return run_width<2>(g, sources, nsrc, d_dist, cc_sum, cc_cnt);
+  return run_width<1>(g, sources, nsrc, d_dist, cc_sum, cc_cnt);
 }
 
 dawn_status bfs_bitset_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc) {

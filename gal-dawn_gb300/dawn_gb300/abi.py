@@ -291,7 +291,7 @@ class Graph:
         _check(lib().dawn_sssp(self.handle, _ptr(s), len(s), _ptr(d), 0, ctypes.byref(st)))
         return d, st
 
-    def closeness(self, sources, weighted=False):
+    def closeness(self, sources, weighted=False, with_stats=False):
         s = np.ascontiguousarray(sources, np.int32)
         cc = np.empty(len(s), np.float64)
         sums = np.empty(len(s), np.float64)
@@ -299,7 +299,7 @@ class Graph:
         st = Stats()
         _check(lib().dawn_closeness(self.handle, _ptr(s), len(s), int(weighted), _ptr(cc), _ptr(sums),
                                     _ptr(reached), ctypes.byref(st)))
-        return cc, sums, reached
+        return (cc, sums, reached, st) if with_stats else (cc, sums, reached)
 
     # -- traversals (device buffers, e.g. torch tensors' data_ptr()) --
     def bfs_device(self, sources, d_dist, variant=VARIANT_AUTO, stats=True):
