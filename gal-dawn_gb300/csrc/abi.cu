@@ -13,6 +13,51 @@
 
 using dawn::DevBuf;
 
+namespace dawn {
+
+// Whether this call's decide kernels evaluate the selector, and with which
+// weights in the handle's slot: the handle's own (dawn_graph_set_selector),
+// else for DAWN_VARIANT_LEARNED the library's trained defaults, else none
+// (direction heuristics).
+dawn_status call_selector(dawn_graph* g, int32_t variant, int32_t* use) {
+  *use = 0;
+  int want = g->sel_on ? 1 : 0;
+#if DAWN_HAVE_DEFAULT_SELECTOR
+  static_assert(sizeof(kDefaultSelectorWeights) == sizeof(float) * DAWN_SELECTOR_WEIGHTS,
+                "default selector weight count");
+  if (!want && variant == DAWN_VARIANT_LEARNED) want = 2;
+#else
+  (void)variant;
+#endif
+  if (!want) return DAWN_OK;
+  if (g->sel_slot_state != want) {
+#if DAWN_HAVE_DEFAULT_SELECTOR
+    const float* src = want == 1 ? g->sel_user.data() : kDefaultSelectorWeights;
+#else
+    const float* src = g->sel_user.data();
+#endif
+    DAWN_CUDA(cudaMemcpyAsync(g->sel_slot.p, src, sizeof(float) * DAWN_SELECTOR_WEIGHTS, cudaMemcpyHostToDevice,
+                              g->stream));
+    DAWN_CUDA(cudaStreamSynchronize(g->stream));
+    g->sel_slot_state = want;
+  }
+  *use = 1;
+  return DAWN_OK;
+}
+
+void drop_graphs(dawn_graph* g) {
+  if (g->stream) cudaStreamSynchronize(g->stream);
+  if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
+  if (g->sssp_exec) cudaGraphExecDestroy(g->sssp_exec);
+  g->bfs_exec = g->sssp_exec = nullptr;
+  for (cudaGraphExec_t& e : g->bs_exec) {
+    if (e) cudaGraphExecDestroy(e);
+    e = nullptr;
+  }
+}
+
+}  // namespace dawn
+
 namespace {
 
 constexpr size_t kStageBytes = (size_t)1 << 31;  // host-pointer calls: device staging per chunk
@@ -110,45 +155,16 @@ void destroy(dawn_graph* g) {
   delete g;
 }
 
-int32_t resolve_variant(int32_t variant, int32_t nsrc) {
-  if (variant == DAWN_VARIANT_AUTO) return nsrc >= 2 ? DAWN_VARIANT_BITSET : DAWN_VARIANT_DO;
+int32_t resolve_variant(const dawn_graph* g, int32_t variant, int32_t nsrc) {
+  if (variant == DAWN_VARIANT_AUTO)
+    return nsrc >= 2 ? (g->auto_learned ? DAWN_VARIANT_LEARNED : DAWN_VARIANT_BITSET) : DAWN_VARIANT_DO;
   return variant;
-}
-
-// Whether this call's decide kernels evaluate the selector, and with which
-// weights in the handle's slot: the handle's own (dawn_graph_set_selector),
-// else for DAWN_VARIANT_LEARNED the library's trained defaults, else none
-// (direction heuristics).
-dawn_status call_selector(dawn_graph* g, int32_t variant, int32_t* use) {
-  *use = 0;
-  int want = g->sel_on ? 1 : 0;
-#if DAWN_HAVE_DEFAULT_SELECTOR
-  static_assert(sizeof(kDefaultSelectorWeights) == sizeof(float) * DAWN_SELECTOR_WEIGHTS,
-                "default selector weight count");
-  if (!want && variant == DAWN_VARIANT_LEARNED) want = 2;
-#else
-  (void)variant;
-#endif
-  if (!want) return DAWN_OK;
-  if (g->sel_slot_state != want) {
-#if DAWN_HAVE_DEFAULT_SELECTOR
-    const float* src = want == 1 ? g->sel_user.data() : kDefaultSelectorWeights;
-#else
-    const float* src = g->sel_user.data();
-#endif
-    DAWN_CUDA(cudaMemcpyAsync(g->sel_slot.p, src, sizeof(float) * DAWN_SELECTOR_WEIGHTS, cudaMemcpyHostToDevice,
-                              g->stream));
-    DAWN_CUDA(cudaStreamSynchronize(g->stream));
-    g->sel_slot_state = want;
-  }
-  *use = 1;
-  return DAWN_OK;
 }
 
 dawn_status bfs_device_impl(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,
                             int32_t variant, dawn_stats* st) {
-  variant = resolve_variant(variant, nsrc);
-  DAWN_CHECK(call_selector(g, variant, &g->sel_call));
+  variant = resolve_variant(g, variant, nsrc);
+  DAWN_CHECK(dawn::call_selector(g, variant, &g->sel_call));
   if (st) {
     std::memset(st, 0, sizeof(*st));
     DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
@@ -425,7 +441,7 @@ dawn_status dawn_bfs(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return DAWN_OK;
   }
-  const int32_t v = resolve_variant(variant, nsrc);
+  const int32_t v = resolve_variant(g, variant, nsrc);
   return staged(
       g, sources, nsrc, dist, sizeof(int32_t), stats,
       [&](const int32_t* s, int32_t c, void* d, dawn_stats* st) {
@@ -500,7 +516,7 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, 
     unsigned long long* d_sum = g->cc_out.as<unsigned long long>();
     unsigned long long* d_cnt = d_sum + nsrc;
     DAWN_CUDA(cudaMemsetAsync(d_sum, 0, 2 * sizeof(unsigned long long) * (size_t)nsrc, g->stream));
-    DAWN_CHECK(call_selector(g, DAWN_VARIANT_BITSET, &g->sel_call));
+    DAWN_CHECK(dawn::call_selector(g, DAWN_VARIANT_BITSET, &g->sel_call));
     if (stats) DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
     DAWN_CHECK(dawn::bfs_bitset(g, sources, nsrc, nullptr, d_sum, d_cnt));
     if (stats) {
@@ -705,10 +721,62 @@ dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value) 
       }
       g->sel_margin = (float)value / 1000.0f;
       return DAWN_OK;
+    case DAWN_OPT_PULL_SEGMENT:
+      if (value < 128 || value > 65536) {
+        dawn::set_error("pull segment must lie in [128, 65536]");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      g->pull_seg = (int32_t)value;  // the pull lists and graphs follow on the next call
+      return DAWN_OK;
+    case DAWN_OPT_BLOCKS_PER_SM:
+      if (value < 0 || value > 32) {
+        dawn::set_error("CTAs per SM must lie in [0, 32]");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      if (g->blocks_per_sm != (int32_t)value) {
+        g->blocks_per_sm = (int32_t)value;
+        dawn::drop_graphs(g);  // grid sizes are part of the captured graphs
+      }
+      return DAWN_OK;
+    case DAWN_OPT_AUTO_LEARNED:
+      if (value != 0 && value != 1) {
+        dawn::set_error("auto-learned must be 0 or 1");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      g->auto_learned = value != 0;
+      return DAWN_OK;
     default:
       dawn::set_error("unknown option %d", option);
       return DAWN_ERR_INVALID_ARG;
   }
+}
+
+dawn_status dawn_autotune(dawn_graph* g, const int32_t* sources, int32_t nsrc, uint32_t flags, dawn_tuning* out) {
+  dawn::clear_error();
+  if (!g || !out || nsrc < 1) {
+    dawn::set_error("autotune needs a graph, at least one source and an output");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  DAWN_CHECK(check_sources(g, sources, nsrc));
+  return dawn::autotune(g, sources, nsrc, flags, out);
+}
+
+dawn_status dawn_tune_cache_save(const char* path) {
+  dawn::clear_error();
+  if (!path) {
+    dawn::set_error("path is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  return dawn::tune_cache_save(path);
+}
+
+dawn_status dawn_tune_cache_load(const char* path) {
+  dawn::clear_error();
+  if (!path) {
+    dawn::set_error("path is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  return dawn::tune_cache_load(path);
 }
 
 dawn_status dawn_graph_set_selector(dawn_graph* g, const float* weights, int32_t count) {
@@ -754,6 +822,15 @@ dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option, int64_t* 
       return DAWN_OK;
     case DAWN_OPT_SELECTOR_MARGIN:
       *value = (int64_t)(g->sel_margin * 1000.0f + 0.5f);
+      return DAWN_OK;
+    case DAWN_OPT_PULL_SEGMENT:
+      *value = g->pull_seg;
+      return DAWN_OK;
+    case DAWN_OPT_BLOCKS_PER_SM:
+      *value = g->blocks_per_sm;
+      return DAWN_OK;
+    case DAWN_OPT_AUTO_LEARNED:
+      *value = g->auto_learned ? 1 : 0;
       return DAWN_OK;
     default:
       dawn::set_error("unknown option %d", option);

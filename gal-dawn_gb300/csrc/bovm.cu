@@ -338,9 +338,9 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   fam.pre[0] = {(const void*)bfs_clear, clear_args, dim3(sms * 4), dim3(kBlock)};
   fam.pre[1] = {(const void*)bfs_init, init_args, dim3(1), dim3(32)};
   fam.nbody = 3;
-  fam.body[0] = {(const void*)bfs_push, push_args, dim3(persistent_blocks((const void*)bfs_push, kBlock, 0)),
+  fam.body[0] = {(const void*)bfs_push, push_args, dim3(persistent_blocks((const void*)bfs_push, kBlock, 0, g->blocks_per_sm)),
                  dim3(kBlock), "bfs_push", kModePush};
-  fam.body[1] = {(const void*)bfs_pull, pull_args, dim3(persistent_blocks((const void*)bfs_pull, kBlock, 0)),
+  fam.body[1] = {(const void*)bfs_pull, pull_args, dim3(persistent_blocks((const void*)bfs_pull, kBlock, 0, g->blocks_per_sm)),
                  dim3(kBlock), "bfs_pull", kModePull};
   fam.body[2] = {(const void*)bfs_decide, decide_args, dim3(1), dim3(32), "bfs_decide"};
   fam.npost = 1;

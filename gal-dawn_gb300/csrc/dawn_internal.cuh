@@ -194,6 +194,10 @@ struct dawn_graph {
   int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges
   int32_t bs_width = 0;         // words per vertex of the bitset traversal (0 = by source count)
   int32_t force_variant = 0;    // 0 = decide per level, else 1 + variant for every level
+  int32_t blocks_per_sm = 0;    // CTAs per SM of the persistent traversal grids (0 = occupancy limit)
+  int32_t pull_seg = 1024;      // heavy pull rows: in-edges per warp task (rows of >= 2x are cut)
+  int32_t static_seg = 0;       // pull_seg the static pull lists were built with
+  bool auto_learned = false;    // DAWN_VARIANT_AUTO batched calls use the learned selector
   // Learned selector.  The decide kernels take the slot's address as a
   // launch argument (fixed for the handle's life, so captured graphs stay
   // valid) and prefetch it while they read the control block.
@@ -237,6 +241,17 @@ namespace dawn {
 // bovm.cu
 dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                        int32_t* d_dist, int32_t policy);
+// abi.cu: whether a call of this variant evaluates the learned selector
+// (and loads its weights into the handle's slot); *use = 0 or 1.
+dawn_status call_selector(dawn_graph* g, int32_t variant, int32_t* use);
+void drop_graphs(dawn_graph* g);
+
+// tune.cu
+dawn_status autotune(dawn_graph* g, const int32_t* sources, int32_t nsrc,
+                     uint32_t flags, dawn_tuning* out);
+dawn_status tune_cache_save(const char* path);
+dawn_status tune_cache_load(const char* path);
+
 // parts.cu
 dawn_status parts_set(dawn_graph* g, int32_t nparts, const int32_t* offsets);
 dawn_status parts_bfs(dawn_graph* g, const int32_t* source_offset,
@@ -266,7 +281,9 @@ dawn_status ss_run(dawn_graph* g, SsFamily& fam, int32_t nsrc,
                    cudaGraphExec_t* exec_cache);
 dawn_status upload_ctl(dawn_graph* g, const SsCtl& c);
 dawn_status download_ctl(dawn_graph* g, SsCtl* out);
-int persistent_blocks(const void* fn, int block, size_t smem);
+// CTAs of a persistent grid: the SM count times the resident CTAs per SM,
+// capped at `cap` per SM when cap > 0.
+int persistent_blocks(const void* fn, int block, size_t smem, int cap = 0);
 dawn_status build_transpose(dawn_graph* g);
 // Per-row reductions over a distance block (kind 0 hops, 1 int32, 2 float):
 // with degree = 0, d_sum gets the exact sum of reached distances of v != s

@@ -248,7 +248,7 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   fam.pre[1] = {(const void*)sssp_init, init_args, dim3(1), dim3(kBlock)};
   fam.nbody = 2;
   fam.body[0] = {(const void*)sssp_relax, relax_args,
-                 dim3(persistent_blocks((const void*)sssp_relax, kBlock, 0)), dim3(kBlock), "sssp_relax"};
+                 dim3(persistent_blocks((const void*)sssp_relax, kBlock, 0, g->blocks_per_sm)), dim3(kBlock), "sssp_relax"};
   fam.body[1] = {(const void*)sssp_decide, decide_args, dim3(1), dim3(32), "sssp_decide"};
   fam.npost = 1;
   fam.post[0] = {(const void*)sssp_next, next_args, dim3(1), dim3(32), "sssp_next"};

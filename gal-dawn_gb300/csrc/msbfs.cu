@@ -69,8 +69,8 @@ struct BsCtl {
 };
 
 constexpr int kSlicesCleared = 4;  // slices zeroed per batch; higher ones on first use
-constexpr int kPullHeavy = 2048;   // in-degree from which a pull row is cut into segments
-constexpr int kPullSeg = 1024;     // entries per heavy-row segment
+// Heavy pull rows: a row of at least 2 x seg in-edges (seg = the handle's
+// pull segment, 1024 by default) is cut into seg-entry warp tasks.
 
 // Words per heavy-row accumulator: W bits and a finished-segment counter,
 // rounded up to an even count so the W words start 16-byte aligned for
@@ -336,8 +336,8 @@ struct LevelAcc {
 };
 
 // Pull: every vertex of the unfinished list ORs the frontier words of its
-// in-neighbours.  Heavy rows (>= kPullHeavy in-edges) come first, one
-// kPullSeg-entry segment per warp task, OR-ed into the row's accumulator;
+// in-neighbours.  Heavy rows (>= 2 x pull_seg in-edges) come first, one
+// pull_seg-entry segment per warp task, OR-ed into the row's accumulator;
 // the warp finishing a row's last segment folds the accumulator into the
 // vertex, so only one warp writes a vertex's words and every segment sees
 // the same visited words for the whole level.  Light rows follow, 32 list
@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kBlock, 4) bs_pull(const int32_t* __restrict__
                                                      const int32_t* __restrict__ ul_static, int32_t ul_static_size,
                                                      int32_t* __restrict__ ul, const int32_t* __restrict__ hv_static,
                                                      const int32_t* __restrict__ hv_segoff, u64* __restrict__ hv_acc,
-                                                     int32_t hv_count, int32_t hv_segs, int32_t n) {
+                                                     int32_t hv_count, int32_t hv_segs, int32_t pull_seg, int32_t n) {
   using B = Bits<W>;
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(kBlock, 4) bs_pull(const int32_t* __restrict__
     const int s0 = __ldg(hv_segoff + lo);
     const int nseg = __ldg(hv_segoff + lo + 1) - s0;
     const int rbeg = t_row_ptr[u], rend = t_row_ptr[u + 1];
-    const int ks = rbeg + (sidx - s0) * kPullSeg, ke = min(ks + kPullSeg, rend);
+    const int ks = rbeg + (sidx - s0) * pull_seg, ke = min(ks + pull_seg, rend);
     u64* hacc = hv_acc + (size_t)lo * acc_stride(W);
     B w = B::zero();
     for (int k0 = ks; k0 < ke; k0 += 128) {
@@ -874,18 +874,18 @@ void probe_bs(const void* p, LevelProbe* out) {
   out->unvisited_edges = c->mu;
 }
 
-// Static pull lists.  Light rows (0 < in-degree < kPullHeavy) are swept in
-// id order, 32 per warp task; heavy rows are cut into kPullSeg-entry
+// Static pull lists.  Light rows (0 < in-degree < 2 x seg) are swept in
+// id order, 32 per warp task; heavy rows are cut into seg-entry
 // segments, one warp task each, so a hub row that cannot stop early is
 // spread over many warps instead of holding one warp for the whole level.
-__global__ void flag_rows(const int32_t* __restrict__ t_row_ptr, int32_t n, int heavy, int64_t* __restrict__ flags,
-                          int64_t* __restrict__ segs) {
+__global__ void flag_rows(const int32_t* __restrict__ t_row_ptr, int32_t n, int heavy, int seg,
+                          int64_t* __restrict__ flags, int64_t* __restrict__ segs) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride) {
     const int d = t_row_ptr[i + 1] - t_row_ptr[i];
-    const bool h = d >= kPullHeavy;
+    const bool h = d >= 2 * seg;
     flags[i] = heavy ? h : (d > 0 && !h);
-    if (segs) segs[i] = h ? (d + kPullSeg - 1) / kPullSeg : 0;
+    if (segs) segs[i] = h ? (d + seg - 1) / seg : 0;
   }
 }
 
@@ -901,7 +901,8 @@ __global__ void scatter_flagged(const int64_t* __restrict__ flags, const int64_t
 }
 
 dawn_status build_static_list(dawn_graph* g) {
-  if (g->ul_static.p) return DAWN_OK;
+  if (g->ul_static.p && g->static_seg == g->pull_seg) return DAWN_OK;
+  const int seg = g->pull_seg;
   const int32_t n = g->n;
   const size_t n1 = (size_t)n + 1;
   int64_t* tmp = nullptr;
@@ -912,7 +913,7 @@ dawn_status build_static_list(dawn_graph* g) {
   DAWN_CHECK(ensure(g->hv_static, sizeof(int32_t) * (size_t)n, g->stream));
   DAWN_CHECK(ensure(g->hv_segoff, sizeof(int32_t) * n1, g->stream));
   for (int heavy = 0; heavy < 2; heavy++) {
-    flag_rows<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->t_row_ptr, n, heavy, flags, heavy ? segs : nullptr);
+    flag_rows<<<g->geo.sms * 4, kBlock, 0, g->stream>>>(g->t_row_ptr, n, heavy, seg, flags, heavy ? segs : nullptr);
     DAWN_CUDA(cudaGetLastError());
     DAWN_CUDA(cudaMemsetAsync(flags + n, 0, sizeof(int64_t), g->stream));
     DAWN_CHECK(exclusive_scan_i64(flags, pos, (int64_t)n1, g->stream));
@@ -940,6 +941,7 @@ dawn_status build_static_list(dawn_graph* g) {
   g->ul_static_size = (int32_t)cnt[0];
   g->hv_count = (int32_t)cnt[1];
   g->hv_segs = (int32_t)nseg;
+  g->static_seg = seg;
   return DAWN_OK;
 }
 
@@ -949,6 +951,15 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   const int32_t n = g->n;
   const size_t nn = (size_t)n;
   const int wi = W == 1 ? 0 : (W == 2 ? 1 : 2);
+  if (g->static_seg != g->pull_seg) {
+    // the pull lists are rebuilt for a new segment size; the captured
+    // graphs hold the old list sizes
+    for (cudaGraphExec_t& e : g->bs_exec)
+      if (e) {
+        cudaGraphExecDestroy(e);
+        e = nullptr;
+      }
+  }
   DAWN_CHECK(build_static_list(g));
   // words (per vertex W each): visit | fr[3] | nxt | level slices[nbits]
   // lists: aq[3] | tq | ul[2] | touched bitmap ; segments[3]
@@ -996,7 +1007,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
     uint32_t* tbm;
     Seg* segs;
     size_t segcap;
-    int32_t ul_static_size, hv_count, hv_segs;
+    int32_t ul_static_size, hv_count, hv_segs, pull_seg;
     const int32_t *hv_static, *hv_segoff;
     u64* hv_acc;
     size_t nwords;
@@ -1019,6 +1030,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   a.hv_acc = g->hv_acc.as<u64>();
   a.hv_count = g->hv_count;
   a.hv_segs = g->hv_segs;
+  a.pull_seg = g->pull_seg;
   a.words = g->bs_words.as<u64>();
   a.visit = a.words;
   a.fr = a.words + W * nn;
@@ -1041,7 +1053,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   void* init_args[] = {&a.ctl, &a.row_ptr, &a.t_row_ptr, &a.visit, &a.fr0, &a.aq0, &a.segs, &a.n, &a.m};
   void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.slices, &a.aq, &a.segs,
                        &a.segcap, &a.ul_static, &a.ul_static_size, &a.ul, &a.hv_static, &a.hv_segoff,
-                       &a.hv_acc, &a.hv_count, &a.hv_segs, &a.n};
+                       &a.hv_acc, &a.hv_count, &a.hv_segs, &a.pull_seg, &a.n};
   void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
                           &a.segcap, &a.tq, &a.tbm, &a.n};
   void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
@@ -1055,13 +1067,13 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   fam.pre[0] = {(const void*)bs_clear, clear_args, dim3(sms * 8), dim3(kBlock), "bs_clear"};
   fam.pre[1] = {(const void*)bs_init<W>, init_args, dim3(1), dim3(64 * W), "bs_init"};
   fam.nbody = 4;
-  fam.body[0] = {(const void*)bs_pull<W>, pull_args, dim3(persistent_blocks((const void*)bs_pull<W>, kBlock, 0)),
+  fam.body[0] = {(const void*)bs_pull<W>, pull_args, dim3(persistent_blocks((const void*)bs_pull<W>, kBlock, 0, g->blocks_per_sm)),
                  dim3(kBlock), "bs_pull", kModePull};
   fam.body[1] = {(const void*)bs_push_scatter<W>, scatter_args,
-                 dim3(persistent_blocks((const void*)bs_push_scatter<W>, kBlock, 0)), dim3(kBlock),
+                 dim3(persistent_blocks((const void*)bs_push_scatter<W>, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
                  "bs_push_scatter", kModePush};
   fam.body[2] = {(const void*)bs_push_update<W>, update_args,
-                 dim3(persistent_blocks((const void*)bs_push_update<W>, kBlock, 0)), dim3(kBlock),
+                 dim3(persistent_blocks((const void*)bs_push_update<W>, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
                  "bs_push_update", kModePush};
   fam.body[3] = {(const void*)bs_decide, decide_args, dim3(1), dim3(32), "bs_decide"};
   fam.npost = 2;

@@ -62,12 +62,13 @@ void release(DevBuf& b) {
   b.bytes = 0;
 }
 
-int persistent_blocks(const void* fn, int block, size_t smem) {
+int persistent_blocks(const void* fn, int block, size_t smem, int cap) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem) != cudaSuccess || per_sm < 1)
     per_sm = 1;
+  if (cap > 0 && cap < per_sm) per_sm = cap;
   return sms * per_sm;
 }
 

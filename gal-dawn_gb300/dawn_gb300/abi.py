@@ -24,10 +24,22 @@ LIB_PATH = os.path.join(LIB_DIR, "libdawn_gb300.so")
 EXPORTS = ("dawn_graph_create", "dawn_graph_create_device", "dawn_graph_destroy",
            "dawn_graph_set_stream", "dawn_graph_synchronize", "dawn_bfs", "dawn_bfs_device", "dawn_bfs_static",
            "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_graph_set_option",
-           "dawn_graph_get_option", "dawn_graph_set_selector", "dawn_graph_set_parts", "dawn_multi_bfs", "dawn_multi_bfs_device",
+           "dawn_graph_get_option", "dawn_graph_set_selector", "dawn_autotune", "dawn_tune_cache_save",
+           "dawn_tune_cache_load", "dawn_graph_set_parts", "dawn_multi_bfs", "dawn_multi_bfs_device",
            "dawn_multi_closeness", "dawn_trace_enable", "dawn_trace_read", "dawn_last_error", "dawn_version")
 OPT_BITSET_WIDTH, OPT_PUSH_RATIO, OPT_FORCE_VARIANT, OPT_SELECTOR_MARGIN = 1, 2, 3, 4
+OPT_PULL_SEGMENT, OPT_BLOCKS_PER_SM, OPT_AUTO_LEARNED = 5, 6, 7
+TUNE_USE_CACHE = 1
 SELECTOR_WEIGHTS = 1475
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("bitset_width", ctypes.c_int32), ("push_ratio", ctypes.c_int32), ("pull_segment", ctypes.c_int32),
+                ("blocks_per_sm", ctypes.c_int32), ("learned", ctypes.c_int32), ("from_cache", ctypes.c_int32),
+                ("ms", ctypes.c_float), ("default_ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class DawnError(RuntimeError):
@@ -83,6 +95,9 @@ def lib():
         L.dawn_graph_set_option.argtypes = [_VP, ctypes.c_int32, ctypes.c_int64]
         L.dawn_graph_get_option.argtypes = [_VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
         L.dawn_graph_set_selector.argtypes = [_VP, _VP, ctypes.c_int32]
+        L.dawn_autotune.argtypes = [_VP, _VP, ctypes.c_int32, ctypes.c_uint32, ctypes.POINTER(Tuning)]
+        L.dawn_tune_cache_save.argtypes = [ctypes.c_char_p]
+        L.dawn_tune_cache_load.argtypes = [ctypes.c_char_p]
         L.dawn_graph_set_parts.argtypes = [_VP, ctypes.c_int32, _VP]
         L.dawn_multi_bfs.argtypes = [_VP, _VP, _VP, _VP, ctypes.POINTER(Stats)]
         L.dawn_multi_bfs_device.argtypes = L.dawn_multi_bfs.argtypes
@@ -192,6 +207,14 @@ class Graph:
         v = ctypes.c_int64()
         _check(lib().dawn_graph_get_option(self.handle, option, ctypes.byref(v)))
         return v.value
+
+    def autotune(self, sources, use_cache=False):
+        """dawn_autotune: measure and set this handle's speed settings."""
+        s = np.ascontiguousarray(sources, np.int32)
+        t = Tuning()
+        _check(lib().dawn_autotune(self.handle, _ptr(s), len(s), TUNE_USE_CACHE if use_cache else 0,
+                                   ctypes.byref(t)))
+        return t.as_dict()
 
     def set_selector(self, weights):
         """dawn_graph_set_selector: load MLP weights (1475 floats) or None."""
@@ -328,6 +351,14 @@ def bfs_static(row_ptr, col, n, m, source, dist, flags=0, stream=None):
     raise DawnError.  Calls that overlap on one device race."""
     _check(lib().dawn_bfs_static(ctypes.c_void_p(row_ptr), ctypes.c_void_p(col), n, m, source,
                                  ctypes.c_void_p(dist), flags, ctypes.c_void_p(stream)))
+
+
+def tune_cache_save(path):
+    _check(lib().dawn_tune_cache_save(os.fsencode(path)))
+
+
+def tune_cache_load(path):
+    _check(lib().dawn_tune_cache_load(os.fsencode(path)))
 
 
 def version():

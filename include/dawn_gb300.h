@@ -224,6 +224,46 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources,
  *                          (default 0: ties go to the heuristic; 250 asks
  *                          for a predicted gain of about 19%). */
 #define DAWN_OPT_SELECTOR_MARGIN 4
+/*   DAWN_OPT_PULL_SEGMENT  in-edges per warp task on heavy pull rows of the
+ *                          batched traversal (rows of at least twice this
+ *                          are spread over several warps); 128..65536,
+ *                          default 1024
+ *   DAWN_OPT_BLOCKS_PER_SM CTAs per SM of the persistent traversal grids:
+ *                          0 = as many as fit (default), else 1..32
+ *   DAWN_OPT_AUTO_LEARNED  1: DAWN_VARIANT_AUTO runs batched calls with the
+ *                          learned selector (as DAWN_VARIANT_LEARNED), 0: with
+ *                          the direction heuristic (default) */
+#define DAWN_OPT_PULL_SEGMENT 5
+#define DAWN_OPT_BLOCKS_PER_SM 6
+#define DAWN_OPT_AUTO_LEARNED 7
+
+/* Autotuner (no counterpart in the reference, whose launch shapes are fixed
+ * in its tools, algorithm/gpu/mssp_gpu/mssp_gpu.cu:16-17).  Times the
+ * traversal of a sample of `sources` (at most 256, distances not written)
+ * under candidate settings, one option at a time: batch width (more than 64
+ * sources), learned selector or heuristic, push ratio, pull segment and
+ * CTAs per SM; keeps the fastest of each and sets them on the handle.
+ * nsrc == 1 tunes the single-source traversal (CTAs per SM only).  The
+ * result is also kept in a process-wide cache keyed by device and graph
+ * class (log2 n, log2 average degree, symmetry, source-count class); with
+ * DAWN_TUNE_USE_CACHE a cached entry is applied without measuring.
+ * Results never depend on the settings. */
+typedef struct dawn_tuning {
+  int32_t bitset_width;   /* 1, 2 or 4 (0: not tuned) */
+  int32_t push_ratio;
+  int32_t pull_segment;
+  int32_t blocks_per_sm;  /* 0: as many as fit */
+  int32_t learned;        /* AUTO batched calls use the learned selector */
+  int32_t from_cache;     /* 1: applied from the cache, nothing measured */
+  float ms;               /* sample time with the chosen settings */
+  float default_ms;       /* sample time with the defaults */
+} dawn_tuning;
+#define DAWN_TUNE_USE_CACHE 1
+dawn_status dawn_autotune(dawn_graph* g, const int32_t* sources, int32_t nsrc,
+                          uint32_t flags, dawn_tuning* out);
+/* Writes / reads the process-wide tuning cache (text, one entry per line). */
+dawn_status dawn_tune_cache_save(const char* path);
+dawn_status dawn_tune_cache_load(const char* path);
 dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value);
 dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option,
                                   int64_t* value);

@@ -64,3 +64,22 @@ def test_sources_in_largest_component():
 
 
 RMAT10_DIGEST = "49028ba9ecab84aa05bc4b8b11571e4c647ea492bcf13cf3f8c59762f05e7a40"
+
+
+def test_tune_cache_file_checks(tmp_path):
+    # host-only: the cache file is parsed and validated without a GPU
+    good = tmp_path / "good.txt"
+    good.write_text("# comment\nGB300|n22|d5|sym|s2 1 4 1024 0 1 2.2 2.25\n")
+    abi.tune_cache_load(str(good))
+    for bad in ("GB300|n22|d5|sym|s2 3 4 1024 0 1 2.2 2.25\n", "x 1 4\n", "k 1 0 1024 0 0 1 1\n"):
+        p = tmp_path / "bad.txt"
+        p.write_text(bad)
+        try:
+            abi.tune_cache_load(str(p))
+        except abi.DawnError as e:
+            assert e.status == abi.ERR_INVALID_ARG
+        else:
+            raise AssertionError("malformed cache accepted: " + bad)
+    out = tmp_path / "out.txt"
+    abi.tune_cache_save(str(out))
+    assert "GB300|n22|d5|sym|s2 1 4 1024 0 1" in out.read_text()
