@@ -392,6 +392,7 @@ def main():
                     help="only the device-resident timing (profiling runs); prints a short JSON line")
     ap.add_argument("--traced", action="store_true",
                     help="with --quick: run the steps level by level, launching only the kernels each level uses")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner before the timed steps")
     ap.add_argument("--variant", default="bitset", choices=["bitset", "learned", "do", "push"])
     ap.add_argument("--suite", action="store_true",
                     help="also time the other workload shapes (one JSON line each, before the main line)")
@@ -440,7 +441,11 @@ def main():
         dg.close()
         return
     # learned + batched: the bitset traversal with each level's variant picked
-    # by the trained selector (the library's default weights)
+    # by the trained selector (the library's default weights); the autotuner
+    # sets the handle's speed options first (untimed, once per graph)
+    tuning = None
+    if not args.no_tune:
+        tuning = dg.autotune(srcs)
     var = HEADLINE_VARIANT(abi)
     step = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=False)  # noqa
     st = dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=True)
@@ -497,6 +502,8 @@ def main():
         t0 = time.perf_counter()
         h = abi.Graph(raw=dict(n=g.n, m=g.m, row_ptr=rp_h.data_ptr(), col=col_h.data_ptr(), symmetric=True,
                                stream=stream))
+        if tuning is not None:
+            h.autotune(srcs, use_cache=True)  # the graph class's tuned settings, nothing measured
         t1 = time.perf_counter()
         h.bfs_host_ptr(srcs, out_h.data_ptr(), variant=var)
         t2 = time.perf_counter()
@@ -535,7 +542,7 @@ def main():
                        "l2": "inputs larger than L2 (CSR %.0f MB, distances %.0f MB per step)" % (
                            (4 * g.m + 4 * g.n) / 2 ** 20, 4 * NSRC * g.n / 2 ** 20),
                        "parallelism": f"sources sharded, {ws} replica(s)"},
-            "clocks": clk, "e2e": e2e, "plain": plain, "batched_heuristic": batched_heuristic,
+            "clocks": clk, "e2e": e2e, "plain": plain, "batched_heuristic": batched_heuristic, "tuning": tuning,
             "speedup_vs_plain": round(value / plain["value"], 3) if plain["value"] else None,
             "roofline": roof, "cpu_baseline": cpu, "gpu_launches": launches * args.steps,
             "levels_per_step": st.levels, "push_levels": st.push_levels, "pull_levels": st.pull_levels}

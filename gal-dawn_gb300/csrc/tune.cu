@@ -31,12 +31,23 @@ struct Settings {
 std::mutex g_cache_mu;
 std::map<std::string, dawn_tuning> g_cache;
 
-std::string class_key(const dawn_graph* g, int32_t nsrc) {
+std::string device_name(int device) {
+  static std::mutex mu;
+  static std::map<int, std::string> names;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = names.find(device);
+  if (it != names.end()) return it->second;
   cudaDeviceProp prop;
   std::string dev = "unknown";
-  if (cudaGetDeviceProperties(&prop, g->device) == cudaSuccess) dev = prop.name;
+  if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) dev = prop.name;
   for (char& c : dev)
     if (c == ' ' || c == '\t' || c == '|') c = '_';
+  names[device] = dev;
+  return dev;
+}
+
+std::string class_key(const dawn_graph* g, int32_t nsrc) {
+  const std::string dev = device_name(g->device);
   const int ln = (int)std::floor(std::log2((double)g->n + 1.0));
   const int ld = (int)std::floor(std::log2((double)g->m / (double)(g->n > 0 ? g->n : 1) + 1.0));
   const int sc = nsrc <= 1 ? 1 : nsrc <= 64 ? 2 : nsrc <= 128 ? 3 : 4;
