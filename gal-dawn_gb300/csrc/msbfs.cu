@@ -684,6 +684,44 @@ __device__ __forceinline__ void emit_vertex(int32_t* __restrict__ dist, int32_t 
   }
 }
 
+// Four consecutive vertices u0..u0+3 per thread: every source row gets one
+// 16-byte store, so a warp writes 512 contiguous bytes per row (needs n and
+// the output base 16-byte aligned, which the caller checks).
+template <int W, int NB>
+__device__ __forceinline__ void emit_vertex4(int32_t* __restrict__ dist, int32_t n, int nb_src, size_t u0,
+                                             const u64* __restrict__ visit, const u64* __restrict__ slices,
+                                             int nbits) {
+#pragma unroll
+  for (int i = 0; i < W; i++) {
+    if (64 * i >= nb_src) break;
+    u64 vis[4];
+    u64 w[NB > 0 ? NB : 1][4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      vis[j] = visit[(u0 + j) * W + i];
+#pragma unroll
+      for (int k = 0; k < NB; k++) w[k][j] = slices[((size_t)k * n + u0 + j) * W + i];
+    }
+    const int cnt = min(64, nb_src - 64 * i);
+    for (int s = 0; s < cnt; s++) {
+      int32_t v[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        v[j] = -1;
+        if ((vis[j] >> s) & 1ull) {
+          int32_t x = 0;
+#pragma unroll
+          for (int k = 0; k < NB; k++) x |= (int32_t)((w[k][j] >> s) & 1ull) << k;
+          for (int k = NB; k < nbits; k++)
+            x |= (int32_t)((slices[((size_t)k * n + u0 + j) * W + i] >> s) & 1ull) << k;
+          v[j] = x;
+        }
+      }
+      *reinterpret_cast<int4*>(dist + (size_t)(64 * i + s) * n + u0) = make_int4(v[0], v[1], v[2], v[3]);
+    }
+  }
+}
+
 // 32 x 32 bit transpose across a warp: lane i holds row i on entry and
 // column i on exit (bit j of lane i's result = bit i of lane j's input).
 __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
@@ -763,6 +801,19 @@ __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__
   const int nbits = 32 - __clz(max(ctl->level, 1));
   int32_t* dist = ctl->dist_base + (size_t)batch * per * n;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if ((n & 3) == 0 && (reinterpret_cast<uintptr_t>(dist) & 15) == 0) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)n / 4; q += stride) {
+      switch (nbits) {
+        case 1: emit_vertex4<W, 1>(dist, n, nb, 4 * q, visit, slices, nbits); break;
+        case 2: emit_vertex4<W, 2>(dist, n, nb, 4 * q, visit, slices, nbits); break;
+        case 3: emit_vertex4<W, 3>(dist, n, nb, 4 * q, visit, slices, nbits); break;
+        case 4: emit_vertex4<W, 4>(dist, n, nb, 4 * q, visit, slices, nbits); break;
+        case 5: emit_vertex4<W, 5>(dist, n, nb, 4 * q, visit, slices, nbits); break;
+        default: emit_vertex4<W, 6>(dist, n, nb, 4 * q, visit, slices, nbits); break;
+      }
+    }
+    return;
+  }
   for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < (size_t)n; u += stride) {
     switch (nbits) {
       case 1: emit_vertex<W, 1>(dist, n, nb, u, visit, slices, nbits); break;
