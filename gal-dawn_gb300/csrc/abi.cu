@@ -138,7 +138,7 @@ void destroy(dawn_graph* g) {
   DevBuf* bufs[] = {&g->ss_queues, &g->ss_segs, &g->bs_segs, &g->ss_bitmaps, &g->ss_ctl, &g->ss_sources, &g->ss_scratch,
                     &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
                     &g->dist_stage, &g->pt_voff, &g->pt_tasks, &g->pt_sources, &g->pt_ctl, &g->pt_scratch, &g->pt_rows,
-                    &g->sel_slot};
+                    &g->sel_slot, &g->wt_col, &g->wt_val};
   for (DevBuf* b : bufs) dawn::release(*b);
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
@@ -211,6 +211,7 @@ dawn_status sssp_device_impl(dawn_graph* g, const int32_t* sources, int32_t nsrc
     DAWN_CHECK(dawn::download_ctl(g, &c));
     st->levels = c.total_levels;
     st->push_levels = c.total_push;
+    st->pull_levels = c.total_pull;
     st->batches = nsrc;
     DAWN_CUDA(cudaEventElapsedTime(&st->device_ms, g->ev0, g->ev1));
     // TEPS numerator: out-degree sum of the reached vertices of every row.

@@ -82,6 +82,8 @@ struct SsCtl {
   int32_t use_sel;              // decide with the handle's selector weights
   int32_t force;                // 0 = decide per level; 1 + variant = always that variant
   float sel_margin;             // log2 margin by which the selector must beat the heuristic
+  int32_t work;                 // weighted pull: dynamic work counter (light rows)
+  int32_t hwork;                // weighted pull: dynamic work counter (heavy-row segments)
   int32_t pad4;
   long long m;                  // CSR entries (selector input)
   // accumulated over all sources of the call
@@ -176,6 +178,8 @@ struct dawn_graph {
   dawn::DevBuf ss_ctl;      // SsCtl
   dawn::DevBuf ss_sources;  // int32 source list of the current call
   dawn::DevBuf ss_scratch;  // n x u64 (GOVM source-row resolution)
+  dawn::DevBuf wt_col;      // weighted in-edge CSR (rows of t_row_ptr): tail vertex
+  dawn::DevBuf wt_val;      // and weight of each in-edge, built on the first weighted pull
   dawn::SsCtl* h_ctl = nullptr;  // pinned: [0] upload staging, [1] download
   bool graphs_ok = true;         // conditional CUDA graphs usable
 
@@ -285,6 +289,10 @@ dawn_status download_ctl(dawn_graph* g, SsCtl* out);
 // capped at `cap` per SM when cap > 0.
 int persistent_blocks(const void* fn, int block, size_t smem, int cap = 0);
 dawn_status build_transpose(dawn_graph* g);
+// In-edge tails and weights in the row layout of t_row_ptr (g->wt_col, g->wt_val).
+dawn_status build_weighted_in_edges(dawn_graph* g);
+// msbfs.cu: light/heavy in-degree lists of the pull kernels (g->ul_static, g->hv_*).
+dawn_status build_static_list(dawn_graph* g);
 // Per-row reductions over a distance block (kind 0 hops, 1 int32, 2 float):
 // with degree = 0, d_sum gets the exact sum of reached distances of v != s
 // (int64 bits for kinds 0/1, float64 for kind 2) and d_cnt their count;

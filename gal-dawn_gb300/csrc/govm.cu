@@ -15,9 +15,16 @@
 //     (src/algorithm/cpu/sssp.cpp:41-46): each distinct neighbour takes the
 //     weight of its last CSR entry, all of them form the first frontier, the
 //     source is set to 0 and is never relaxed afterwards.
-// Any relaxation order reaches the same fixed point, so the distances equal
-// the reference's for integer-valued weights.
+//   * levels whose frontier out-edges exceed m run as a pull instead: every vertex with in-edges takes the minimum of d[u] + w over
+//     its in-edges from last level's frontier (a bitmap test per in-edge,
+//     the gathers only for frontier tails), so the dense levels need no
+//     atomics on light rows; rows of at least 2 x pull_seg in-edges are cut
+//     into warp tasks combined with atomicMin.
+// Any relaxation order reaches the same fixed point (the minimum over paths
+// of the path sums, which rounding leaves monotone), so push, pull and
+// their mix give the distances of the reference CPU path.
 #include "dawn_device.cuh"
+#include "selector.cuh"
 
 namespace dawn {
 namespace {
@@ -28,12 +35,30 @@ __device__ __forceinline__ int32_t relax_sum(int32_t dv, int k, const int32_t* _
   return dv + __ldg(wi + k);
 }
 
+// Pull when a level's frontier out-edges exceed m, a full in-edge scan.  On
+// RMAT scale 22 the pull was not faster than the push at any level (1.05 vs
+// 1.08 ms at the 126M-edge level, 0.84 vs 0.43 ms at the 58M-edge one), so
+// it is kept for frontiers heavier than the graph.
+constexpr long long kPullRatio = 1;
+
+// Frontier bitmaps rotate over three slots: level L reads slot (L-1)%3 (the
+// vertices level L-1 improved), writes slot L%3 and clears slot (L+1)%3,
+// which no kernel of level L reads or writes.
+__device__ __forceinline__ uint32_t* slot_of(uint32_t* bm, int i, int32_t nwords) {
+  return bm + (size_t)(i % 3) * nwords;
+}
+
+__device__ __forceinline__ void clear_slot(uint32_t* __restrict__ w, int32_t nwords) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += stride) w[i] = 0;
+}
+
 __global__ void __launch_bounds__(kBlock) sssp_clear(SsCtl* __restrict__ ctl, uint32_t* __restrict__ inq,
                                                      int32_t n, int32_t nwords, int32_t inf) {
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride) dist[i] = inf;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)2 * nwords; i += stride) inq[i] = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)3 * nwords; i += stride) inq[i] = 0;
 }
 
 // One CTA: resolve the source row (last CSR entry of a repeated neighbour
@@ -42,7 +67,7 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
                                                     const int32_t* __restrict__ col, const int32_t* __restrict__ wi,
                                                     const float* __restrict__ wf, int is_float,
                                                     unsigned long long* __restrict__ last, int32_t* __restrict__ q,
-                                                    Seg* __restrict__ segs, int32_t n) {
+                                                    Seg* __restrict__ segs, uint32_t* __restrict__ inq, int32_t n) {
   const int32_t s = ctl->sources[ctl->src_idx];
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
   const int rs = row_ptr[s], re = row_ptr[s + 1];
@@ -56,6 +81,11 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
     ctl->n_push = 0;
     ctl->n_pull = 0;
     ctl->reached = 0;
+    ctl->mf[0] = 0;
+    ctl->mf[1] = 0;
+    ctl->work = 0;
+    ctl->hwork = 0;
+    ctl->mode = ctl->force - 1 == kVarPull ? kModePull : kModePush;
   }
   for (int k = rs + threadIdx.x; k < re; k += blockDim.x) last[col[k]] = 0;
   __syncthreads();
@@ -65,8 +95,10 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
     const int32_t u = col[k];
     if (last[u] == (unsigned long long)(k + 1)) {
       dist[u] = is_float ? __float_as_int(__ldg(wf + k)) : __ldg(wi + k);
-      // winners are unique: no dedup bit needed
+      // winners are unique; the bit marks u in the level-0 frontier slot
+      atomicOr(inq + (u >> 5), 1u << (u & 31));
       const int urs = row_ptr[u], udeg = row_ptr[u + 1] - urs;
+      atomicAdd(&ctl->mf[0], (unsigned long long)udeg);
       if (udeg >= kLongRow) {
         const int nseg = (udeg + kSeg - 1) / kSeg;
         const unsigned long long old = atomicAdd(&ctl->lpack[0], (1ull << 32) | (unsigned)nseg);
@@ -93,7 +125,7 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
   __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
-  if (ctl->done) return;
+  if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
   const int32_t* qin = q + (size_t)pin * n;
@@ -102,22 +134,16 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
   Seg* sout = segs + (size_t)pout * segcap;
   unsigned long long* lpack = &ctl->lpack[pout];
   const int ln = seg_count(ctl->lpack[pin]);
-  uint32_t* inq_in = inq + (size_t)pin * nwords;
-  uint32_t* inq_out = inq + (size_t)pout * nwords;
+  uint32_t* inq_out = slot_of(inq, L, nwords);
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
   int32_t* qcount = &ctl->qsize[pout];
   const int32_t source = ctl->source;
   const int qn = ctl->qsize[pin];
   const int wib = threadIdx.x >> 5;
 
-  // The input queue's dedup bits are free again once the level has started:
-  // this level claims in inq_out only.
-  const size_t gstride = (size_t)gridDim.x * blockDim.x;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)(qn + ln); i += gstride) {
-    const int32_t v = i < (size_t)qn ? qin[i] : sin[i - qn].v;
-    atomicAnd(inq_in + (v >> 5), ~(1u << (v & 31)));
-  }
+  clear_slot(slot_of(inq, L + 1, nwords), nwords);
 
+  unsigned long long my_mf = 0;
   WarpQueue wq(s_q[wib], qout, qcount);
   auto op = [&](int32_t v, int k, bool valid) {
     bool found = false;
@@ -136,22 +162,163 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
     if (found) {
       rs = row_ptr[u];
       deg = row_ptr[u + 1] - rs;
+      my_mf += (unsigned long long)deg;
     }
     emit_routed(found, u, deg, rs, wq, sout, lpack);
   };
   seg_expand(row_ptr, sin, ln, op);
   warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
   wq.flush();
+  my_mf = warp_sum(my_mf);
+  if (lane_id() == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }
 
-__global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop, int in_graph) {
+// Pull level: every vertex with in-edges takes the minimum of d[u] + w over
+// in-edges whose tail u is in last level's frontier.  Heavy rows (>= 2 x
+// pull_seg in-edges) come first as pull_seg-entry warp tasks, combined by
+// atomicMin on the distance; light rows follow, 32 vertices per warp task,
+// each owned by its warp (plain store): rows of >= 32 in-edges swept by the
+// whole warp, shorter ones concatenated across the lanes and combined with
+// shared-memory atomicMin.  Improved vertices form the next frontier (queue
+// and bitmap slot), long rows as segments.
+__global__ void __launch_bounds__(kBlock) sssp_pull(const int32_t* __restrict__ row_ptr,
+                                                    const int32_t* __restrict__ t_row_ptr,
+                                                    const int32_t* __restrict__ t_col,
+                                                    const int32_t* __restrict__ t_wi, const float* __restrict__ t_wf,
+                                                    int is_float, SsCtl* __restrict__ ctl, int32_t* __restrict__ q,
+                                                    Seg* __restrict__ segs, size_t segcap,
+                                                    uint32_t* __restrict__ inq, const int32_t* __restrict__ ul,
+                                                    int32_t ul_n, const int32_t* __restrict__ hv,
+                                                    const int32_t* __restrict__ hv_segoff, int32_t hv_count,
+                                                    int32_t hv_segs, int32_t pull_seg, int32_t n, int32_t nwords) {
+  __shared__ int s_excl[kBlock / 32][32];
+  __shared__ int s_rs[kBlock / 32][32];
+  __shared__ int32_t s_min[kBlock / 32][32];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  if (ctl->done || ctl->mode != kModePull) return;
+  const int L = ctl->level;
+  const int pout = L & 1;
+  const uint32_t* fin = slot_of(inq, L - 1, nwords);
+  uint32_t* fout = slot_of(inq, L, nwords);
+  clear_slot(slot_of(inq, L + 1, nwords), nwords);
+  int32_t* qout = q + (size_t)pout * n;
+  Seg* sout = segs + (size_t)pout * segcap;
+  unsigned long long* lpack = &ctl->lpack[pout];
+  int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
+  const int lane = lane_id(), wib = threadIdx.x >> 5;
+  const bool fl = is_float != 0;
+  unsigned long long my_mf = 0;
+  WarpQueue wq(s_q[wib], qout, &ctl->qsize[pout]);
+
+  for (;;) {
+    int sidx = 0;
+    if (lane == 0) sidx = atomicAdd(&ctl->hwork, 1);
+    sidx = __shfl_sync(kFull, sidx, 0);
+    if (sidx >= hv_segs) break;
+    int lo = 0, hi = hv_count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(hv_segoff + mid) <= sidx) lo = mid; else hi = mid - 1;
+    }
+    const int32_t v = __ldg(hv + lo);
+    const int rbeg = t_row_ptr[v], rend = t_row_ptr[v + 1];
+    const int ks = rbeg + (sidx - __ldg(hv_segoff + lo)) * pull_seg, ke = min(ks + pull_seg, rend);
+    int32_t best = 0x7fffffff;
+    for (int k = ks + lane; k < ke; k += 32) {
+      const int32_t u = __ldg(t_col + k);
+      if ((__ldcg(fin + (u >> 5)) >> (u & 31)) & 1u) best = min(best, relax_sum(__ldcg(dist + u), k, t_wi, t_wf, fl));
+    }
+    best = __reduce_min_sync(kFull, best);
+    bool found = false;
+    int deg = 0, rs = 0;
+    if (lane == 0 && best < __ldcg(dist + v)) {
+      const int32_t old = atomicMin(dist + v, best);
+      if (best < old && claim_bit(fout, v)) {
+        found = true;
+        rs = row_ptr[v];
+        deg = row_ptr[v + 1] - rs;
+        my_mf += (unsigned long long)deg;
+      }
+    }
+    emit_routed(found, v, deg, rs, wq, sout, lpack);
+  }
+
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctl->work, 32);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= ul_n) break;
+    const int idx = base + lane;
+    int32_t v = -1;
+    int rs = 0, re = 0;
+    if (idx < ul_n) {
+      v = __ldg(ul + idx);
+      rs = t_row_ptr[v];
+      re = t_row_ptr[v + 1];
+    }
+    const int deg = re - rs;
+    int32_t best = 0x7fffffff;
+    uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
+    while (big) {
+      const int leader = __ffs(big) - 1;
+      big &= big - 1;
+      const int s = __shfl_sync(kFull, rs, leader), e = __shfl_sync(kFull, re, leader);
+      int32_t b = 0x7fffffff;
+      for (int k = s + lane; k < e; k += 32) {
+        const int32_t u = __ldg(t_col + k);
+        if ((__ldcg(fin + (u >> 5)) >> (u & 31)) & 1u) b = min(b, relax_sum(__ldcg(dist + u), k, t_wi, t_wf, fl));
+      }
+      b = __reduce_min_sync(kFull, b);
+      if (lane == leader) best = b;
+    }
+    const int sdeg = deg < kWarpRow ? deg : 0;
+    const int incl = warp_incl_scan(sdeg);
+    const int total = __shfl_sync(kFull, incl, 31);
+    s_excl[wib][lane] = incl - sdeg;
+    s_rs[wib][lane] = rs;
+    s_min[wib][lane] = 0x7fffffff;
+    __syncwarp();
+    for (int e = lane; e < total; e += 32) {
+      int lo = 0, hi = 31;
+#pragma unroll
+      for (int it = 0; it < 5; it++) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_excl[wib][mid] <= e) lo = mid; else hi = mid - 1;
+      }
+      const int k = s_rs[wib][lo] + (e - s_excl[wib][lo]);
+      const int32_t u = __ldg(t_col + k);
+      if ((__ldcg(fin + (u >> 5)) >> (u & 31)) & 1u)
+        atomicMin(&s_min[wib][lo], relax_sum(__ldcg(dist + u), k, t_wi, t_wf, fl));
+    }
+    __syncwarp();
+    if (sdeg > 0) best = s_min[wib][lane];
+    __syncwarp();
+    bool found = false;
+    int odeg = 0, ors = 0;
+    if (v >= 0 && best < __ldcg(dist + v)) {
+      dist[v] = best;  // this warp owns v's light row
+      atomicOr(fout + (v >> 5), 1u << (v & 31));
+      found = true;
+      ors = row_ptr[v];
+      odeg = row_ptr[v + 1] - ors;
+      my_mf += (unsigned long long)odeg;
+    }
+    emit_routed(found, v, odeg, ors, wq, sout, lpack);
+  }
+  wq.flush();
+  my_mf = warp_sum(my_mf);
+  if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
+}
+
+__global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, int can_pull, cudaGraphConditionalHandle loop,
+                            int in_graph) {
   if (threadIdx.x != 0) return;
   if (ctl->done) {
     if (in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
   const int L = ctl->level, pout = L & 1;
-  ctl->n_push++;
+  if (ctl->mode == kModePush) ctl->n_push++; else ctl->n_pull++;
   // The reference stops after n levels at most (src/algorithm/cpu/sssp.cpp:34);
   // with non-negative weights the queue empties long before.
   if ((ctl->qsize[pout] == 0 && ctl->lpack[pout] == 0) || L >= n) {
@@ -161,6 +328,13 @@ __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, cudaGraphConditi
   }
   ctl->qsize[pout ^ 1] = 0;
   ctl->lpack[pout ^ 1] = 0;
+  ctl->mf[pout ^ 1] = 0;
+  ctl->work = 0;
+  ctl->hwork = 0;
+  int mode = (long long)ctl->mf[pout] * kPullRatio > ctl->m ? kModePull : kModePush;
+  if (ctl->force) mode = ctl->force - 1 == kVarPull ? kModePull : kModePush;
+  if (!can_pull) mode = kModePush;
+  ctl->mode = mode;
   ctl->level = L + 1;
 }
 
@@ -168,16 +342,17 @@ __global__ void sssp_next(SsCtl* __restrict__ ctl) {
   if (threadIdx.x != 0) return;
   ctl->total_levels += ctl->level;
   ctl->total_push += ctl->n_push;
+  ctl->total_pull += ctl->n_pull;
   ctl->src_idx += 1;
 }
 
 void probe_sssp(const void* p, LevelProbe* out) {
   const SsCtl* c = static_cast<const SsCtl*>(p);
   out->level = c->level;
-  out->mode = kModePush;
+  out->mode = c->mode;
   out->done = c->done;
   out->frontier = c->qsize[(c->level - 1) & 1] + (int64_t)(c->lpack[(c->level - 1) & 1] >> 32);
-  out->frontier_edges = 0;
+  out->frontier_edges = (int64_t)c->mf[(c->level - 1) & 1];
   out->unvisited_edges = 0;
 }
 
@@ -193,11 +368,20 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   DAWN_CHECK(ensure(g->ss_scratch, sizeof(unsigned long long) * (size_t)n, g->stream));
   DAWN_CHECK(ensure(g->ss_ctl, sizeof(SsCtl), g->stream));
   DAWN_CHECK(ensure(g->ss_sources, sizeof(int32_t) * (size_t)nsrc, g->stream));
+  // pull levels read in-edges with their weights and the in-degree lists
+  if (g->static_seg != g->pull_seg && g->sssp_exec) {
+    cudaGraphExecDestroy(g->sssp_exec);  // its pull launch holds the old list sizes
+    g->sssp_exec = nullptr;
+  }
+  DAWN_CHECK(build_weighted_in_edges(g));
+  DAWN_CHECK(build_static_list(g));
   DAWN_CUDA(cudaMemcpyAsync(g->ss_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
                             g->stream));
   const int is_float = g->wtype == DAWN_W_F32;
   SsCtl c = {};
   c.policy = DAWN_VARIANT_PUSH;
+  c.force = g->force_variant == 3 ? 1 + kVarPush : g->force_variant;
+  c.m = g->m;
   c.weighted = is_float;
   c.nsrc = nsrc;
   c.dist_base = static_cast<int32_t*>(d_dist);
@@ -217,7 +401,22 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
     int32_t n, nwords, inf;
     cudaGraphConditionalHandle handle;
     int in_graph;
+    const int32_t *t_row_ptr, *t_col, *t_wi, *ul, *hv, *hv_segoff;
+    const float* t_wf;
+    int32_t ul_n, hv_count, hv_segs, pull_seg, can_pull;
   } a;
+  a.t_row_ptr = g->t_row_ptr;
+  a.t_col = g->wt_col.as<int32_t>();
+  a.t_wi = is_float ? nullptr : g->wt_val.as<int32_t>();
+  a.t_wf = is_float ? g->wt_val.as<float>() : nullptr;
+  a.ul = g->ul_static.as<int32_t>();
+  a.hv = g->hv_static.as<int32_t>();
+  a.hv_segoff = g->hv_segoff.as<int32_t>();
+  a.ul_n = g->ul_static_size;
+  a.hv_count = g->hv_count;
+  a.hv_segs = g->hv_segs;
+  a.pull_seg = g->pull_seg;
+  a.can_pull = 1;
   a.ctl = g->ss_ctl.as<SsCtl>();
   a.row_ptr = g->row_ptr;
   a.col = g->col;
@@ -235,10 +434,13 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   a.handle = 0;
   a.in_graph = 0;
   void* clear_args[] = {&a.ctl, &a.inq, &a.n, &a.nwords, &a.inf};
-  void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.last, &a.q, &a.segs, &a.n};
+  void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.last, &a.q, &a.segs, &a.inq, &a.n};
   void* relax_args[] = {&a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.ctl, &a.q, &a.segs, &a.segcap,
                         &a.inq, &a.n, &a.nwords};
-  void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
+  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.t_wi, &a.t_wf, &a.is_float, &a.ctl, &a.q, &a.segs,
+                       &a.segcap, &a.inq, &a.ul, &a.ul_n, &a.hv, &a.hv_segoff, &a.hv_count, &a.hv_segs,
+                       &a.pull_seg, &a.n, &a.nwords};
+  void* decide_args[] = {&a.ctl, &a.n, &a.can_pull, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
 
   const int sms = g->geo.sms;
@@ -246,10 +448,14 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   fam.npre = 2;
   fam.pre[0] = {(const void*)sssp_clear, clear_args, dim3(sms * 4), dim3(kBlock)};
   fam.pre[1] = {(const void*)sssp_init, init_args, dim3(1), dim3(kBlock)};
-  fam.nbody = 2;
+  fam.nbody = 3;
   fam.body[0] = {(const void*)sssp_relax, relax_args,
-                 dim3(persistent_blocks((const void*)sssp_relax, kBlock, 0, g->blocks_per_sm)), dim3(kBlock), "sssp_relax"};
-  fam.body[1] = {(const void*)sssp_decide, decide_args, dim3(1), dim3(32), "sssp_decide"};
+                 dim3(persistent_blocks((const void*)sssp_relax, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
+                 "sssp_relax", kModePush};
+  fam.body[1] = {(const void*)sssp_pull, pull_args,
+                 dim3(persistent_blocks((const void*)sssp_pull, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
+                 "sssp_pull", kModePull};
+  fam.body[2] = {(const void*)sssp_decide, decide_args, dim3(1), dim3(32), "sssp_decide"};
   fam.npost = 1;
   fam.post[0] = {(const void*)sssp_next, next_args, dim3(1), dim3(32), "sssp_next"};
   fam.ctl = a.ctl;

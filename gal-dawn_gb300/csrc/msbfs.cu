@@ -951,6 +951,9 @@ __global__ void scatter_flagged(const int64_t* __restrict__ flags, const int64_t
     }
 }
 
+}  // namespace
+
+// Static pull lists of the in-edge CSR (shared with the weighted pull).
 dawn_status build_static_list(dawn_graph* g) {
   if (g->ul_static.p && g->static_seg == g->pull_seg) return DAWN_OK;
   const int seg = g->pull_seg;
@@ -995,6 +998,8 @@ dawn_status build_static_list(dawn_graph* g) {
   g->static_seg = seg;
   return DAWN_OK;
 }
+
+namespace {
 
 template <int W>
 dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,

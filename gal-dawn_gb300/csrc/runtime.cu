@@ -418,7 +418,49 @@ __global__ void scatter_in_edges(const int32_t* __restrict__ rp, const int32_t* 
   }
 }
 
+__global__ void init_cursor(const int32_t* __restrict__ t_row_ptr, unsigned long long* __restrict__ cursor,
+                            int32_t n) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride)
+    cursor[i] = (unsigned long long)t_row_ptr[i];
+}
+
+__global__ void scatter_weighted_in_edges(const int32_t* __restrict__ rp, const int32_t* __restrict__ col,
+                                          const int32_t* __restrict__ val, int32_t n,
+                                          unsigned long long* __restrict__ cursor, int32_t* __restrict__ t_col,
+                                          int32_t* __restrict__ t_val) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += warps) {
+    const int e = rp[u + 1];
+    for (int k = rp[u] + lane; k < e; k += 32) {
+      const unsigned long long slot = atomicAdd(cursor + col[k], 1ull);
+      t_col[slot] = u;
+      t_val[slot] = val[k];
+    }
+  }
+}
+
 }  // namespace
+
+dawn_status build_weighted_in_edges(dawn_graph* g) {
+  if (g->wt_col.p) return DAWN_OK;
+  const int32_t n = g->n;
+  const cudaStream_t s = g->stream;
+  unsigned long long* cursor = nullptr;
+  DAWN_CHECK(pool_alloc((void**)&cursor, sizeof(unsigned long long) * ((size_t)n + 1), s));
+  DAWN_CHECK(ensure(g->wt_col, sizeof(int32_t) * (size_t)(g->m > 0 ? g->m : 1) + 16, s));
+  DAWN_CHECK(ensure(g->wt_val, sizeof(int32_t) * (size_t)(g->m > 0 ? g->m : 1) + 16, s));
+  const int grid = g->geo.sms * 8;
+  init_cursor<<<grid, kBlock, 0, s>>>(g->t_row_ptr, cursor, n);
+  DAWN_CUDA(cudaGetLastError());
+  // 32-bit weights (int32 or float32 bit patterns) move as words
+  scatter_weighted_in_edges<<<grid, kBlock, 0, s>>>(g->row_ptr, g->col, static_cast<const int32_t*>(g->val), n,
+                                                    cursor, g->wt_col.as<int32_t>(), g->wt_val.as<int32_t>());
+  DAWN_CUDA(cudaGetLastError());
+  pool_free(cursor, s);
+  return DAWN_OK;
+}
 
 dawn_status build_transpose(dawn_graph* g) {
   const int32_t n = g->n;

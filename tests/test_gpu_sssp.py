@@ -91,3 +91,48 @@ def test_long_rows_weighted():
     # symmetric weights are not needed for SSSP parity
     g.w_i32, g.w_f32 = w, w.astype(np.float32)
     check(g, np.array([0, 5, 1300], np.int32))
+
+
+def asym_weights(g, seed):
+    """Same topology, weights drawn per directed entry (so w(u,v) != w(v,u)):
+    a pull level must read in-edge weights, not mirror the out-edges."""
+    rng = np.random.default_rng(seed)
+    wi = rng.integers(1, 64, g.m).astype(np.int32)
+    return gen.CsrGraph(g.n, g.row_ptr, g.col, wi, wi.astype(np.float32), symmetric=g.symmetric)
+
+
+@pytest.mark.parametrize("force", [1, 2, 0])
+def test_forced_push_and_pull(force):
+    # every level as push (1), every level as pull (2), or chosen per level
+    # (0): the distances are the oracle's in each case
+    graphs = [
+        asym_weights(gen.rmat(14, 16, seed=61), 62),           # symmetric topology, asymmetric weights
+        gen.erdos_renyi(20000, 200000, seed=63, weights=True),  # directed
+        gen.rmat(16, 32, a=0.62, b=0.17, c=0.17, seed=64, weights=True),  # hubs: segmented pull rows
+    ]
+    for g in graphs:
+        srcs = gen.sources(g, 5, seed=65, from_lcc=g.symmetric)
+        want = O.msssp(g, srcs)
+        for w in ("i32", "f32"):
+            with abi.Graph(g, weights=w) as dg:
+                dg.set_option(abi.OPT_FORCE_VARIANT, force)
+                d, st = dg.sssp(srcs)
+                got = to_ref(d)
+                bad = np.argwhere(got != want)
+                assert bad.size == 0, (force, w, g.n, bad[:5])
+                if force == 2:
+                    assert st.pull_levels > 0
+                if force == 1:
+                    assert st.pull_levels == 0
+
+
+def test_pull_segment_sizes():
+    g = gen.rmat(16, 32, a=0.62, b=0.17, c=0.17, seed=66, weights=True)
+    srcs = gen.sources(g, 3, seed=67)
+    want = O.msssp(g, srcs)
+    with abi.Graph(g, weights="i32") as dg:
+        dg.set_option(abi.OPT_FORCE_VARIANT, 2)
+        for seg in (128, 1024, 8192):
+            dg.set_option(abi.OPT_PULL_SEGMENT, seg)
+            d, _ = dg.sssp(srcs)
+            assert np.array_equal(to_ref(d), want), seg
