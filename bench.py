@@ -314,11 +314,12 @@ def suite_lines(torch, abi, gen, stream, rank):
     for w in ("i32", "f32"):
         with abi.Graph(g, weights=w, stream=stream) as dg:
             d = torch.empty((NSRC, g.n), dtype=torch.int32, device="cuda")
-            st = dg.sssp_device(srcs, d.data_ptr())
-            ms = timed(lambda: dg.sssp_device(srcs, d.data_ptr(), stats=False), 2)
-            out.append({"suite": "rmat22-sssp-64src", "weights": w, "ms_per_step": round(ms, 3),
-                        "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2),
-                        "levels_per_source": round(st.levels / NSRC, 1)})
+            for var, name in ((abi.VARIANT_AUTO, "batched (64 sources per traversal)"),
+                              (abi.VARIANT_DO, "single-source")):
+                st = dg.sssp_device(srcs, d.data_ptr(), variant=var)
+                ms = timed(lambda: dg.sssp_device(srcs, d.data_ptr(), stats=False, variant=var), 2)
+                out.append({"suite": "rmat22-sssp-64src", "weights": w, "variant": name, "ms_per_step": round(ms, 3),
+                            "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2), "levels": st.levels})
     del g
     # RMAT-18, 4096 sources
     g = gen.rmat(18, EDGEFACTOR, A, B, C, seed=GRAPH_SEED)

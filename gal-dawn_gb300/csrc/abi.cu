@@ -49,7 +49,8 @@ void drop_graphs(dawn_graph* g) {
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
   if (g->sssp_exec) cudaGraphExecDestroy(g->sssp_exec);
-  g->bfs_exec = g->sssp_exec = nullptr;
+  if (g->mw_exec) cudaGraphExecDestroy(g->mw_exec);
+  g->bfs_exec = g->sssp_exec = g->mw_exec = nullptr;
   for (cudaGraphExec_t& e : g->bs_exec) {
     if (e) cudaGraphExecDestroy(e);
     e = nullptr;
@@ -138,7 +139,8 @@ void destroy(dawn_graph* g) {
   DevBuf* bufs[] = {&g->ss_queues, &g->ss_segs, &g->bs_segs, &g->ss_bitmaps, &g->ss_ctl, &g->ss_sources, &g->ss_scratch,
                     &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
                     &g->dist_stage, &g->pt_voff, &g->pt_tasks, &g->pt_sources, &g->pt_ctl, &g->pt_scratch, &g->pt_rows,
-                    &g->sel_slot, &g->wt_col, &g->wt_val};
+                    &g->sel_slot, &g->wt_col, &g->wt_val, &g->mw_block, &g->mw_masks,
+                    &g->mw_ctl, &g->mw_sources};
   for (DevBuf* b : bufs) dawn::release(*b);
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
@@ -146,6 +148,7 @@ void destroy(dawn_graph* g) {
   for (cudaGraphExec_t e : g->bs_exec)
     if (e) cudaGraphExecDestroy(e);
   if (g->pt_exec) cudaGraphExecDestroy(g->pt_exec);
+  if (g->mw_exec) cudaGraphExecDestroy(g->mw_exec);
   if (g->h_ctl) cudaFreeHost(g->h_ctl);
   for (cudaEvent_t e : g->trace_ev)
     if (e) cudaEventDestroy(e);
@@ -198,11 +201,26 @@ dawn_status bfs_device_impl(dawn_graph* g, const int32_t* sources, int32_t nsrc,
   return DAWN_OK;
 }
 
+// Batched (64 sources per traversal) unless the caller asks for the
+// single-source kernels or there is one source.
+bool sssp_uses_batch(int32_t variant, int32_t nsrc) {
+  return nsrc >= 2 && variant != DAWN_VARIANT_PUSH && variant != DAWN_VARIANT_DO;
+}
+
 dawn_status sssp_device_impl(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist,
-                             dawn_stats* st) {
+                             dawn_stats* st, int32_t variant = DAWN_VARIANT_AUTO) {
   if (st) {
     std::memset(st, 0, sizeof(*st));
     DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
+  }
+  if (sssp_uses_batch(variant, nsrc)) {
+    DAWN_CHECK(dawn::sssp_batched(g, sources, nsrc, d_dist));
+    if (st) {
+      DAWN_CUDA(cudaEventRecord(g->ev1, g->stream));
+      DAWN_CHECK(dawn::sssp_batched_stats(g, st, nsrc));
+      DAWN_CUDA(cudaEventElapsedTime(&st->device_ms, g->ev0, g->ev1));
+    }
+    return DAWN_OK;
   }
   DAWN_CHECK(dawn::sssp_single(g, sources, nsrc, d_dist));
   if (st) {
@@ -454,7 +472,6 @@ dawn_status dawn_bfs(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_
 dawn_status dawn_sssp_device(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist, int32_t variant,
                              dawn_stats* stats) {
   dawn::clear_error();
-  (void)variant;
   if (!g || (nsrc > 0 && !d_dist)) {
     dawn::set_error("graph or distance buffer is NULL");
     return DAWN_ERR_INVALID_ARG;
@@ -468,13 +485,12 @@ dawn_status dawn_sssp_device(dawn_graph* g, const int32_t* sources, int32_t nsrc
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return DAWN_OK;
   }
-  return sssp_device_impl(g, sources, nsrc, d_dist, stats);
+  return sssp_device_impl(g, sources, nsrc, d_dist, stats, variant);
 }
 
 dawn_status dawn_sssp(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* dist, int32_t variant,
                       dawn_stats* stats) {
   dawn::clear_error();
-  (void)variant;
   if (!g) {
     dawn::set_error("graph is NULL");
     return DAWN_ERR_INVALID_ARG;
@@ -488,10 +504,10 @@ dawn_status dawn_sssp(dawn_graph* g, const int32_t* sources, int32_t nsrc, void*
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return DAWN_OK;
   }
-  return staged(g, sources, nsrc, dist, sizeof(int32_t), stats,
-                [&](const int32_t* s, int32_t c, void* d, dawn_stats* st) {
-                  return sssp_device_impl(g, s, c, d, st);
-                });
+  return staged(
+      g, sources, nsrc, dist, sizeof(int32_t), stats,
+      [&](const int32_t* s, int32_t c, void* d, dawn_stats* st) { return sssp_device_impl(g, s, c, d, st, variant); },
+      sssp_uses_batch(variant, nsrc));
 }
 
 dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t weighted, double* cc,

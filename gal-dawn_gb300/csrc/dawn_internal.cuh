@@ -178,6 +178,10 @@ struct dawn_graph {
   dawn::DevBuf ss_ctl;      // SsCtl
   dawn::DevBuf ss_sources;  // int32 source list of the current call
   dawn::DevBuf ss_scratch;  // n x u64 (GOVM source-row resolution)
+  dawn::DevBuf mw_block;    // batched weighted traversal: n x 64 int32 distances
+  dawn::DevBuf mw_masks;    // 3 x n uint64 improved-source masks
+  dawn::DevBuf mw_ctl;
+  dawn::DevBuf mw_sources;
   dawn::DevBuf wt_col;      // weighted in-edge CSR (rows of t_row_ptr): tail vertex
   dawn::DevBuf wt_val;      // and weight of each in-edge, built on the first weighted pull
   dawn::SsCtl* h_ctl = nullptr;  // pinned: [0] upload staging, [1] download
@@ -230,6 +234,8 @@ struct dawn_graph {
   cudaGraphExec_t bfs_exec = nullptr;
   cudaGraphExec_t sssp_exec = nullptr;
   int32_t sssp_exec_weighted = -1;
+  cudaGraphExec_t mw_exec = nullptr;  // batched weighted traversal
+  int32_t mw_exec_float = -1;
   cudaGraphExec_t bs_exec[3] = {nullptr, nullptr, nullptr};  // bitset width 1, 2, 4
 
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -255,6 +261,11 @@ dawn_status autotune(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                      uint32_t flags, dawn_tuning* out);
 dawn_status tune_cache_save(const char* path);
 dawn_status tune_cache_load(const char* path);
+
+// msssp.cu: weighted distances of up to 64 sources per batched traversal
+// (d_dist nsrc x n, the single-source encoding)
+dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist);
+dawn_status sssp_batched_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc);
 
 // parts.cu
 dawn_status parts_set(dawn_graph* g, int32_t nparts, const int32_t* offsets);

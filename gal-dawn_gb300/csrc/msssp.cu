@@ -1,0 +1,389 @@
+// Batched min-plus relax: weighted distances from up to 64 sources in one
+// traversal, on sm_103a.
+//
+// The reference computes weighted multi-source distances one source at a
+// time (MSSP_GPU::run_Weighted, src/algorithm/gpu/mssp.cu:53-102), each a
+// full GOVM traversal that re-reads the CSR and pays one atomic per
+// improving edge.  Here a batch of up to 64 sources shares one traversal:
+//   * distances live vertex-major, 64 int32 words per vertex (int32 weights
+//     natively, float32 through their bit pattern, which orders like the
+//     value for the non-negative floats the upload admits), so the 64
+//     distances of an edge's head are one 256-byte row;
+//   * the frontier is a queue of vertices with a 64-bit mask per vertex of
+//     the sources whose distance improved at the last level (three mask
+//     slots rotate by level % 3: level L reads (L-1)%3, writes L%3, clears
+//     (L+1)%3);
+//   * a warp takes one frontier vertex (rows of >= 128 entries one
+//     128-entry segment at a time); lane i owns sources i and i + 32.  The
+//     warp loads 32 of the row's targets and weights in one coalesced read,
+//     then for each edge every lane relaxes its two sources against the
+//     target's distance row and applies atomicMin only where it improves;
+//     the improved sources are OR-ed into the target's next mask, and the
+//     first setter queues the target;
+//   * a final pass transposes the block into the caller's source-major rows
+//     and counts the reached edges.
+// Each source's first frontier is resolved as the single-source path does
+// (the reference CPU path, src/algorithm/cpu/sssp.cpp:41-46): each distinct
+// neighbour takes the weight of its last CSR entry, the source is set to 0
+// and is relaxed again only through a self loop.  Any relaxation order
+// reaches the same fixed point, so the distances equal the single-source
+// traversal's.
+#include "dawn_device.cuh"
+
+namespace dawn {
+namespace {
+
+constexpr int kBatch = 64;  // sources per batch (two per lane)
+constexpr int kUnroll = 4;  // edges whose distance rows are fetched together
+
+struct MwCtl {
+  int32_t qsize[2];
+  unsigned long long lpack[2];
+  unsigned long long mf[2];
+  int32_t level, done, batch, nsrc;
+  int32_t n_push, pad0;
+  unsigned long long reached;   // TEPS numerator of all batches so far
+  int32_t* dist_base;           // nsrc x n output (source-major)
+  const int32_t* sources;
+  int32_t total_levels, total_push;
+};
+
+__device__ __forceinline__ int32_t relax(int32_t d, int32_t w, bool is_float) {
+  if (is_float) return __float_as_int(__fadd_rn(__int_as_float(d), __int_as_float(w)));
+  return d + w;
+}
+
+__global__ void __launch_bounds__(kBlock) mw_clear(int32_t* __restrict__ D, size_t words, int32_t inf,
+                                                   unsigned long long* __restrict__ masks, size_t nmask) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  int4* d4 = reinterpret_cast<int4*>(D);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < words / 4; i += stride)
+    d4[i] = make_int4(inf, inf, inf, inf);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nmask; i += stride) masks[i] = 0ull;
+}
+
+// One CTA: the batch's sources one after another.  For source b, each
+// distinct neighbour takes the weight of its last CSR entry (an atomicMax
+// on the entry position picks it), enters the level-0 mask with bit b and
+// is queued by its first setter; then the source's own entry is set to 0.
+__global__ void __launch_bounds__(1024) mw_init(MwCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
+                                                const int32_t* __restrict__ col, const int32_t* __restrict__ w,
+                                                int32_t* __restrict__ D, unsigned long long* __restrict__ mask0,
+                                                unsigned long long* __restrict__ last, int32_t* __restrict__ q,
+                                                Seg* __restrict__ segs, int32_t n) {
+  const int batch = ctl->batch;
+  const int nb = min(kBatch, ctl->nsrc - batch * kBatch);
+  if (threadIdx.x == 0) {
+    ctl->qsize[0] = ctl->qsize[1] = 0;
+    ctl->lpack[0] = ctl->lpack[1] = 0;
+    ctl->mf[0] = ctl->mf[1] = 0;
+    ctl->level = 1;
+    ctl->done = 0;
+    ctl->n_push = 0;
+  }
+  __syncthreads();
+  for (int b = 0; b < nb; b++) {
+    const int32_t s = ctl->sources[batch * kBatch + b];
+    const int rs = row_ptr[s], re = row_ptr[s + 1];
+    for (int k = rs + threadIdx.x; k < re; k += blockDim.x) last[col[k]] = 0;
+    __syncthreads();
+    for (int k = rs + threadIdx.x; k < re; k += blockDim.x) atomicMax(last + col[k], (unsigned long long)(k + 1));
+    __syncthreads();
+    for (int k = rs + threadIdx.x; k < re; k += blockDim.x) {
+      const int32_t u = col[k];
+      if (last[u] != (unsigned long long)(k + 1)) continue;
+      D[(size_t)u * kBatch + b] = __ldg(w + k);
+      const unsigned long long old = atomicOr(mask0 + u, 1ull << b);
+      if (old == 0ull) {
+        const int urs = row_ptr[u], udeg = row_ptr[u + 1] - urs;
+        atomicAdd(&ctl->mf[0], (unsigned long long)udeg);
+        if (udeg >= kLongRow) {
+          const int nseg = (udeg + kSeg - 1) / kSeg;
+          const unsigned long long o = atomicAdd(&ctl->lpack[0], (1ull << 32) | (unsigned)nseg);
+          for (int j = 0; j < nseg; j++) segs[(uint32_t)o + j] = Seg{u, urs + j * kSeg};
+        } else {
+          q[atomicAdd(&ctl->qsize[0], 1)] = u;
+        }
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) D[(size_t)s * kBatch + b] = 0;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) ctl->done = ctl->qsize[0] == 0 && ctl->lpack[0] == 0;
+}
+
+// One level.  Warp tasks: the long-row segments, then the short-row
+// vertices of the input queue (grid-stride over warps).
+__global__ void __launch_bounds__(kBlock) mw_push(const int32_t* __restrict__ row_ptr,
+                                                  const int32_t* __restrict__ col, const int32_t* __restrict__ w,
+                                                  int is_float, MwCtl* __restrict__ ctl, int32_t* __restrict__ D,
+                                                  unsigned long long* __restrict__ masks, int32_t* __restrict__ q,
+                                                  Seg* __restrict__ segs, size_t segcap, int32_t n) {
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  if (ctl->done) return;
+  const int L = ctl->level;
+  const int pin = (L - 1) & 1, pout = L & 1;
+  const unsigned long long* __restrict__ m_in = masks + (size_t)((L - 1) % 3) * n;
+  unsigned long long* m_out = masks + (size_t)(L % 3) * n;
+  {
+    unsigned long long* m_clr = masks + (size_t)((L + 1) % 3) * n;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride) m_clr[i] = 0ull;
+  }
+  const int32_t* qin = q + (size_t)pin * n;
+  const Seg* sin = segs + (size_t)pin * segcap;
+  const int qn = ctl->qsize[pin];
+  const int ln = seg_count(ctl->lpack[pin]);
+  const int lane = lane_id(), wib = threadIdx.x >> 5;
+  const bool fl = is_float != 0;
+  WarpQueue wq(s_q[wib], q + (size_t)pout * n, &ctl->qsize[pout]);
+  Seg* sout = segs + (size_t)pout * segcap;
+  unsigned long long* lpack = &ctl->lpack[pout];
+  unsigned long long my_mf = 0;
+
+  for (int t = global_warp(); t < ln + qn; t += num_warps()) {
+    int32_t u;
+    int k0, k1;
+    if (t < ln) {
+      const Seg sg = sin[t];
+      u = sg.v;
+      k0 = sg.k0;
+      k1 = min(k0 + kSeg, row_ptr[u + 1]);
+    } else {
+      u = qin[t - ln];
+      k0 = row_ptr[u];
+      k1 = row_ptr[u + 1];
+    }
+    const unsigned long long mask = __ldcg(m_in + u);
+    const bool actA = (mask >> lane) & 1ull, actB = (mask >> (lane + 32)) & 1ull;
+    const int32_t* du = D + (size_t)u * kBatch;
+    const int32_t dA = __ldcg(du + lane), dB = __ldcg(du + lane + 32);
+    for (int kb = k0; kb < k1; kb += 32) {
+      const int k = kb + lane;
+      const int32_t cv = k < k1 ? __ldg(col + k) : -1;
+      const int32_t cw = k < k1 ? __ldg(w + k) : 0;
+      const int cnt = min(32, k1 - kb);
+      // Lane j collects the improved sources of edge kb + j (its own edge),
+      // so the next-mask update and the queue append run once per 32 edges.
+      unsigned long long mybits = 0ull;
+      // kUnroll edges at a time: their distance rows are all loaded, then
+      // all atomics issued, before the first ballot
+      for (int j0 = 0; j0 < cnt; j0 += kUnroll) {
+        int32_t v[kUnroll], wv[kUnroll], curA[kUnroll], curB[kUnroll];
+#pragma unroll
+        for (int i = 0; i < kUnroll; i++) {
+          v[i] = __shfl_sync(kFull, cv, (j0 + i) & 31);
+          wv[i] = __shfl_sync(kFull, cw, (j0 + i) & 31);
+          if (j0 + i >= cnt) v[i] = -1;
+        }
+#pragma unroll
+        for (int i = 0; i < kUnroll; i++) {
+          const int32_t* dv = D + (size_t)(v[i] < 0 ? 0 : v[i]) * kBatch;
+          curA[i] = (v[i] >= 0 && actA) ? __ldcg(dv + lane) : 0;
+          curB[i] = (v[i] >= 0 && actB) ? __ldcg(dv + lane + 32) : 0;
+        }
+        bool impA[kUnroll], impB[kUnroll];
+#pragma unroll
+        for (int i = 0; i < kUnroll; i++) {
+          impA[i] = impB[i] = false;
+          if (v[i] < 0) continue;
+          int32_t* dv = D + (size_t)v[i] * kBatch;
+          if (actA) {
+            const int32_t c = relax(dA, wv[i], fl);
+            if (c < curA[i]) impA[i] = c < atomicMin(dv + lane, c);
+          }
+          if (actB) {
+            const int32_t c = relax(dB, wv[i], fl);
+            if (c < curB[i]) impB[i] = c < atomicMin(dv + lane + 32, c);
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < kUnroll; i++) {
+          const unsigned long long bits = (unsigned long long)__ballot_sync(kFull, impA[i]) |
+                                          ((unsigned long long)__ballot_sync(kFull, impB[i]) << 32);
+          if (lane == j0 + i) mybits = bits;
+        }
+      }
+      bool first = false;
+      int deg = 0, rs = 0;
+      if (mybits) {
+        first = atomicOr(m_out + cv, mybits) == 0ull;
+        if (first) {
+          rs = row_ptr[cv];
+          deg = row_ptr[cv + 1] - rs;
+          my_mf += (unsigned long long)deg;
+        }
+      }
+      emit_routed(first, cv, deg, rs, wq, sout, lpack);
+    }
+  }
+  wq.flush();
+  my_mf = warp_sum(my_mf);
+  if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
+}
+
+__global__ void mw_decide(MwCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop, int in_graph) {
+  if (threadIdx.x != 0) return;
+  if (ctl->done) {
+    if (in_graph) cudaGraphSetConditional(loop, 0);
+    return;
+  }
+  const int L = ctl->level, pout = L & 1;
+  ctl->n_push++;
+  if ((ctl->qsize[pout] == 0 && ctl->lpack[pout] == 0) || L >= n) {
+    ctl->done = 1;
+    if (in_graph) cudaGraphSetConditional(loop, 0);
+    return;
+  }
+  ctl->qsize[pout ^ 1] = 0;
+  ctl->lpack[pout ^ 1] = 0;
+  ctl->mf[pout ^ 1] = 0;
+  ctl->level = L + 1;
+}
+
+// Block -> the batch's source-major rows; each vertex adds its out-degree
+// once per source that reached it (TEPS numerator).
+__global__ void __launch_bounds__(kBlock) mw_emit(MwCtl* __restrict__ ctl, const int32_t* __restrict__ D,
+                                                  const int32_t* __restrict__ row_ptr, int32_t inf, int32_t n) {
+  const int batch = ctl->batch;
+  const int nb = min(kBatch, ctl->nsrc - batch * kBatch);
+  int32_t* dist = ctl->dist_base + (size_t)batch * kBatch * n;
+  unsigned long long reached = 0;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < (size_t)n; v += stride) {
+    const int4* row = reinterpret_cast<const int4*>(D + v * kBatch);
+    int cnt = 0;
+    for (int c = 0; c < nb; c += 4) {
+      const int4 x = __ldcs(row + c / 4);
+      const int32_t xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (c + j < nb) {
+          dist[(size_t)(c + j) * n + v] = xs[j];
+          cnt += xs[j] != inf;
+        }
+    }
+    reached += (unsigned long long)cnt * (unsigned long long)(row_ptr[v + 1] - row_ptr[v]);
+  }
+  reached = warp_sum(reached);
+  if (lane_id() == 0 && reached) atomicAdd(&ctl->reached, reached);
+}
+
+__global__ void mw_next(MwCtl* __restrict__ ctl) {
+  if (threadIdx.x != 0) return;
+  ctl->total_levels += ctl->level;
+  ctl->total_push += ctl->n_push;
+  ctl->batch += 1;
+}
+
+void probe_mw(const void* p, LevelProbe* out) {
+  const MwCtl* c = static_cast<const MwCtl*>(p);
+  const int pin = (c->level - 1) & 1;
+  out->level = c->level;
+  out->mode = kModePush;
+  out->done = c->done;
+  out->frontier = c->qsize[pin] + (int64_t)(c->lpack[pin] >> 32);
+  out->frontier_edges = (int64_t)c->mf[pin];
+  out->unvisited_edges = 0;
+}
+
+}  // namespace
+
+dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist) {
+  const int32_t n = g->n;
+  const size_t nn = (size_t)n;
+  const int is_float = g->wtype == DAWN_W_F32;
+  const size_t segcap = seg_capacity(n, g->m);
+  DAWN_CHECK(ensure(g->mw_block, sizeof(int32_t) * kBatch * nn, g->stream));
+  DAWN_CHECK(ensure(g->mw_masks, sizeof(unsigned long long) * 3 * nn, g->stream));
+  DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * nn, g->stream));
+  DAWN_CHECK(ensure(g->ss_segs, sizeof(Seg) * 2 * segcap, g->stream));
+  DAWN_CHECK(ensure(g->ss_scratch, sizeof(unsigned long long) * nn, g->stream));
+  DAWN_CHECK(ensure(g->mw_ctl, sizeof(MwCtl), g->stream));
+  DAWN_CHECK(ensure(g->mw_sources, sizeof(int32_t) * (size_t)nsrc, g->stream));
+  DAWN_CUDA(cudaMemcpyAsync(g->mw_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
+                            g->stream));
+  MwCtl c = {};
+  c.nsrc = nsrc;
+  c.dist_base = static_cast<int32_t*>(d_dist);
+  c.sources = g->mw_sources.as<int32_t>();
+  DAWN_CUDA(cudaMemcpyAsync(g->mw_ctl.p, &c, sizeof(MwCtl), cudaMemcpyHostToDevice, g->stream));
+
+  struct {
+    MwCtl* ctl;
+    const int32_t *row_ptr, *col, *w;
+    int is_float;
+    int32_t* D;
+    unsigned long long *masks, *last;
+    int32_t* q;
+    Seg* segs;
+    size_t segcap, words, nmask;
+    int32_t n, inf;
+    cudaGraphConditionalHandle handle;
+    int in_graph;
+  } a;
+  a.ctl = g->mw_ctl.as<MwCtl>();
+  a.row_ptr = g->row_ptr;
+  a.col = g->col;
+  a.w = static_cast<const int32_t*>(g->val);  // int32 weights or float32 bit patterns
+  a.is_float = is_float;
+  a.D = g->mw_block.as<int32_t>();
+  a.masks = g->mw_masks.as<unsigned long long>();
+  a.last = g->ss_scratch.as<unsigned long long>();
+  a.q = g->ss_queues.as<int32_t>();
+  a.segs = g->ss_segs.as<Seg>();
+  a.segcap = segcap;
+  a.words = kBatch * nn;
+  a.nmask = 3 * nn;
+  a.n = n;
+  a.inf = is_float ? 0x7f7fffff : 0x7fffffff;  // FLT_MAX bits / INT32_MAX
+  a.handle = 0;
+  a.in_graph = 0;
+  void* clear_args[] = {&a.D, &a.words, &a.inf, &a.masks, &a.nmask};
+  void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.w, &a.D, &a.masks, &a.last, &a.q, &a.segs, &a.n};
+  void* push_args[] = {&a.row_ptr, &a.col, &a.w, &a.is_float, &a.ctl, &a.D, &a.masks, &a.q, &a.segs, &a.segcap,
+                       &a.n};
+  void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
+  void* emit_args[] = {&a.ctl, &a.D, &a.row_ptr, &a.inf, &a.n};
+  void* next_args[] = {&a.ctl};
+  const int sms = g->geo.sms;
+  SsFamily fam;
+  fam.npre = 2;
+  fam.pre[0] = {(const void*)mw_clear, clear_args, dim3(sms * 8), dim3(kBlock), "mw_clear"};
+  fam.pre[1] = {(const void*)mw_init, init_args, dim3(1), dim3(1024), "mw_init"};
+  fam.nbody = 2;
+  fam.body[0] = {(const void*)mw_push, push_args,
+                 dim3(persistent_blocks((const void*)mw_push, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
+                 "mw_push", kModePush};
+  fam.body[1] = {(const void*)mw_decide, decide_args, dim3(1), dim3(32), "mw_decide"};
+  fam.npost = 2;
+  fam.post[0] = {(const void*)mw_emit, emit_args, dim3(sms * 8), dim3(kBlock), "mw_emit"};
+  fam.post[1] = {(const void*)mw_next, next_args, dim3(1), dim3(32), "mw_next"};
+  fam.ctl = a.ctl;
+  fam.ctl_bytes = sizeof(MwCtl);
+  fam.probe = probe_mw;
+  fam.handle = &a.handle;
+  fam.in_graph = &a.in_graph;
+  fam.done_flag = &a.ctl->done;
+  if (g->mw_exec && g->mw_exec_float != is_float) {
+    cudaGraphExecDestroy(g->mw_exec);
+    g->mw_exec = nullptr;
+  }
+  g->mw_exec_float = is_float;
+  return ss_run(g, fam, (nsrc + kBatch - 1) / kBatch, &g->mw_exec);
+}
+
+dawn_status sssp_batched_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc) {
+  MwCtl h;
+  DAWN_CUDA(cudaMemcpyAsync(&h, g->mw_ctl.p, sizeof(MwCtl), cudaMemcpyDeviceToHost, g->stream));
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  st->edges_traversed = (int64_t)h.reached;
+  st->levels = h.total_levels;
+  st->push_levels = h.total_push;
+  st->pull_levels = 0;
+  st->batches = (nsrc + kBatch - 1) / kBatch;
+  return DAWN_OK;
+}
+
+}  // namespace dawn

@@ -306,12 +306,14 @@ class Graph:
         _check(lib().dawn_bfs(self.handle, _ptr(s), len(s), _ptr(d), variant, ctypes.byref(st)))
         return d, st
 
-    def sssp(self, sources, out=None):
+    def sssp(self, sources, out=None, variant=VARIANT_AUTO):
+        """Weighted distances; AUTO batches 64 sources per traversal, DO/PUSH
+        run the single-source kernels."""
         s = np.ascontiguousarray(sources, np.int32)
         dt = np.float32 if self.wtype == W_F32 else np.int32
         d = out if out is not None else np.empty((len(s), self.n), dt)
         st = Stats()
-        _check(lib().dawn_sssp(self.handle, _ptr(s), len(s), _ptr(d), 0, ctypes.byref(st)))
+        _check(lib().dawn_sssp(self.handle, _ptr(s), len(s), _ptr(d), variant, ctypes.byref(st)))
         return d, st
 
     def closeness(self, sources, weighted=False, with_stats=False):
@@ -332,10 +334,10 @@ class Graph:
                                      ctypes.byref(st) if st is not None else None))
         return st
 
-    def sssp_device(self, sources, d_dist, stats=True):
+    def sssp_device(self, sources, d_dist, stats=True, variant=VARIANT_AUTO):
         s = np.ascontiguousarray(sources, np.int32)
         st = Stats() if stats else None
-        _check(lib().dawn_sssp_device(self.handle, _ptr(s), len(s), ctypes.c_void_p(d_dist), 0,
+        _check(lib().dawn_sssp_device(self.handle, _ptr(s), len(s), ctypes.c_void_p(d_dist), variant,
                                       ctypes.byref(st) if st is not None else None))
         return st
 

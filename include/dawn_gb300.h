@@ -180,7 +180,11 @@ dawn_status dawn_multi_closeness(dawn_graph* g, const int32_t* source_offset,
  * MSSP_GPU::run_Weighted (src/algorithm/gpu/mssp.cu:53-102).  The source's
  * own row initialises its neighbours with the last CSR entry of a repeated
  * neighbour, as the reference CPU path does (src/algorithm/cpu/sssp.cpp:41-45).
- * As with dawn_bfs, a NULL dist returns only the statistics. */
+ * As with dawn_bfs, a NULL dist returns only the statistics.
+ * variant: DAWN_VARIANT_PUSH or DAWN_VARIANT_DO run one traversal per
+ * source; any other value (AUTO) runs two or more sources 64 per batched
+ * traversal (a vertex-major 64-distance block, one relaxation pass per
+ * edge for all sources of the batch).  The distances are the same. */
 dawn_status dawn_sssp(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                       void* dist, int32_t variant, dawn_stats* stats);
 dawn_status dawn_sssp_device(dawn_graph* g, const int32_t* sources,

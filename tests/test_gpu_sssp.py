@@ -17,15 +17,18 @@ def to_ref(d):
 
 
 def check(g, srcs, weights=("i32", "f32")):
+    # AUTO runs the batched traversal (64 sources per pass) for two or more
+    # sources, DO the single-source kernels; both must give the oracle's
     want = O.msssp(g, srcs)
     for w in weights:
         with abi.Graph(g, weights=w) as dg:
-            d, st = dg.sssp(srcs)
-            got = to_ref(d)
-            bad = np.argwhere(got != want)
-            assert bad.size == 0, (w, bad[:5])
-            reached = want != abi.FLT_MAX
-            assert st.edges_traversed == int((reached * g.degrees()[None, :]).sum())
+            for variant in (abi.VARIANT_AUTO, abi.VARIANT_DO):
+                d, st = dg.sssp(srcs, variant=variant)
+                got = to_ref(d)
+                bad = np.argwhere(got != want)
+                assert bad.size == 0, (w, variant, bad[:5])
+                reached = want != abi.FLT_MAX
+                assert st.edges_traversed == int((reached * g.degrees()[None, :]).sum()), variant
 
 
 def test_golden(goldens):
@@ -62,6 +65,7 @@ def test_source_row_duplicates_last_wins():
     want = O.msssp(g, [0])
     assert want.tolist() == [[0.0, 5.0, 6.0]]
     check(g, [0])
+    check(g, [0, 0, 1])  # batched: every source bit resolves its row alone
 
 
 def test_source_self_loop_is_expanded():
@@ -74,6 +78,7 @@ def test_source_self_loop_is_expanded():
     want = O.msssp(g, [0])
     assert want.tolist() == [[0.0, 3.0, 4.0]]
     check(g, [0])
+    check(g, [0, 2, 0])
 
 
 def test_unweighted_graph_rejected():
@@ -116,7 +121,7 @@ def test_forced_push_and_pull(force):
         for w in ("i32", "f32"):
             with abi.Graph(g, weights=w) as dg:
                 dg.set_option(abi.OPT_FORCE_VARIANT, force)
-                d, st = dg.sssp(srcs)
+                d, st = dg.sssp(srcs, variant=abi.VARIANT_DO)
                 got = to_ref(d)
                 bad = np.argwhere(got != want)
                 assert bad.size == 0, (force, w, g.n, bad[:5])
@@ -134,5 +139,21 @@ def test_pull_segment_sizes():
         dg.set_option(abi.OPT_FORCE_VARIANT, 2)
         for seg in (128, 1024, 8192):
             dg.set_option(abi.OPT_PULL_SEGMENT, seg)
-            d, _ = dg.sssp(srcs)
+            d, _ = dg.sssp(srcs, variant=abi.VARIANT_DO)
             assert np.array_equal(to_ref(d), want), seg
+
+
+def test_batched_many_sources():
+    # 150 sources: three batches (the last ragged), duplicates, isolated
+    # sources and sources in other components
+    g = gen.rmat(13, 8, seed=71, weights=True)
+    iso = np.nonzero(g.degrees() == 0)[0]
+    s = gen.sources(g, 140, seed=72)
+    srcs = np.concatenate([s[:100], s[:5], iso[:3], s[100:]]).astype(np.int32)
+    check(g, srcs)
+
+
+def test_batched_directed_asymmetric():
+    g = asym_weights(gen.erdos_renyi(5000, 60000, seed=73), 74)
+    g = gen.CsrGraph(g.n, g.row_ptr, g.col, g.w_i32, g.w_f32, symmetric=False)
+    check(g, gen.sources(g, 70, seed=75, from_lcc=False))
