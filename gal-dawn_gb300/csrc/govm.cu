@@ -115,17 +115,13 @@ __global__ void __launch_bounds__(kBlock) sssp_init(SsCtl* __restrict__ ctl, con
   }
 }
 
-__global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__ row_ptr,
+__device__ __forceinline__ void push_level(int* s_excl, int* s_rs, int* s_v, int32_t* s_q,
+                                           const int32_t* __restrict__ row_ptr,
                                                      const int32_t* __restrict__ col, const int32_t* __restrict__ wi,
                                                      const float* __restrict__ wf, int is_float,
                                                      SsCtl* __restrict__ ctl, int32_t* __restrict__ q,
                                                      Seg* __restrict__ segs, size_t segcap,
                                                      uint32_t* __restrict__ inq, int32_t n, int32_t nwords) {
-  __shared__ int s_excl[kBlock / 32][32];
-  __shared__ int s_rs[kBlock / 32][32];
-  __shared__ int s_v[kBlock / 32][32];
-  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
-  if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
   const int32_t* qin = q + (size_t)pin * n;
@@ -144,7 +140,7 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
   clear_slot(slot_of(inq, L + 1, nwords), nwords);
 
   unsigned long long my_mf = 0;
-  WarpQueue wq(s_q[wib], qout, qcount);
+  WarpQueue wq(s_q, qout, qcount);
   auto op = [&](int32_t v, int k, bool valid) {
     bool found = false;
     int32_t u = -1;
@@ -167,7 +163,7 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
     emit_routed(found, u, deg, rs, wq, sout, lpack);
   };
   seg_expand(row_ptr, sin, ln, op);
-  warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
+  warp_expand(row_ptr, qin, qn, s_excl, s_rs, s_v, op);
   wq.flush();
   my_mf = warp_sum(my_mf);
   if (lane_id() == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
@@ -181,7 +177,8 @@ __global__ void __launch_bounds__(kBlock) sssp_relax(const int32_t* __restrict__
 // whole warp, shorter ones concatenated across the lanes and combined with
 // shared-memory atomicMin.  Improved vertices form the next frontier (queue
 // and bitmap slot), long rows as segments.
-__global__ void __launch_bounds__(kBlock) sssp_pull(const int32_t* __restrict__ row_ptr,
+__device__ __forceinline__ void pull_level(int* s_excl, int* s_rs, int32_t* s_min, int32_t* s_q,
+                                           const int32_t* __restrict__ row_ptr,
                                                     const int32_t* __restrict__ t_row_ptr,
                                                     const int32_t* __restrict__ t_col,
                                                     const int32_t* __restrict__ t_wi, const float* __restrict__ t_wf,
@@ -191,11 +188,6 @@ __global__ void __launch_bounds__(kBlock) sssp_pull(const int32_t* __restrict__ 
                                                     int32_t ul_n, const int32_t* __restrict__ hv,
                                                     const int32_t* __restrict__ hv_segoff, int32_t hv_count,
                                                     int32_t hv_segs, int32_t pull_seg, int32_t n, int32_t nwords) {
-  __shared__ int s_excl[kBlock / 32][32];
-  __shared__ int s_rs[kBlock / 32][32];
-  __shared__ int32_t s_min[kBlock / 32][32];
-  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
-  if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
   const int pout = L & 1;
   const uint32_t* fin = slot_of(inq, L - 1, nwords);
@@ -208,7 +200,7 @@ __global__ void __launch_bounds__(kBlock) sssp_pull(const int32_t* __restrict__ 
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   const bool fl = is_float != 0;
   unsigned long long my_mf = 0;
-  WarpQueue wq(s_q[wib], qout, &ctl->qsize[pout]);
+  WarpQueue wq(s_q, qout, &ctl->qsize[pout]);
 
   for (;;) {
     int sidx = 0;
@@ -274,24 +266,24 @@ __global__ void __launch_bounds__(kBlock) sssp_pull(const int32_t* __restrict__ 
     const int sdeg = deg < kWarpRow ? deg : 0;
     const int incl = warp_incl_scan(sdeg);
     const int total = __shfl_sync(kFull, incl, 31);
-    s_excl[wib][lane] = incl - sdeg;
-    s_rs[wib][lane] = rs;
-    s_min[wib][lane] = 0x7fffffff;
+    s_excl[lane] = incl - sdeg;
+    s_rs[lane] = rs;
+    s_min[lane] = 0x7fffffff;
     __syncwarp();
     for (int e = lane; e < total; e += 32) {
       int lo = 0, hi = 31;
 #pragma unroll
       for (int it = 0; it < 5; it++) {
         const int mid = (lo + hi + 1) >> 1;
-        if (s_excl[wib][mid] <= e) lo = mid; else hi = mid - 1;
+        if (s_excl[mid] <= e) lo = mid; else hi = mid - 1;
       }
-      const int k = s_rs[wib][lo] + (e - s_excl[wib][lo]);
+      const int k = s_rs[lo] + (e - s_excl[lo]);
       const int32_t u = __ldg(t_col + k);
       if ((__ldcg(fin + (u >> 5)) >> (u & 31)) & 1u)
-        atomicMin(&s_min[wib][lo], relax_sum(__ldcg(dist + u), k, t_wi, t_wf, fl));
+        atomicMin(&s_min[lo], relax_sum(__ldcg(dist + u), k, t_wi, t_wf, fl));
     }
     __syncwarp();
-    if (sdeg > 0) best = s_min[wib][lane];
+    if (sdeg > 0) best = s_min[lane];
     __syncwarp();
     bool found = false;
     int odeg = 0, ors = 0;
@@ -308,6 +300,35 @@ __global__ void __launch_bounds__(kBlock) sssp_pull(const int32_t* __restrict__ 
   wq.flush();
   my_mf = warp_sum(my_mf);
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
+}
+
+// One level: the push or the pull body, as the decide kernel chose, in one
+// launch per level.
+__global__ void __launch_bounds__(kBlock, 6) sssp_step(const int32_t* __restrict__ row_ptr,
+                                                    const int32_t* __restrict__ col, const int32_t* __restrict__ wi,
+                                                    const float* __restrict__ wf, int is_float,
+                                                    SsCtl* __restrict__ ctl, int32_t* __restrict__ q,
+                                                    Seg* __restrict__ segs, size_t segcap,
+                                                    uint32_t* __restrict__ inq, int32_t n, int32_t nwords,
+                                                    const int32_t* __restrict__ t_row_ptr,
+                                                    const int32_t* __restrict__ t_col,
+                                                    const int32_t* __restrict__ t_wi, const float* __restrict__ t_wf,
+                                                    const int32_t* __restrict__ ul, int32_t ul_n,
+                                                    const int32_t* __restrict__ hv,
+                                                    const int32_t* __restrict__ hv_segoff, int32_t hv_count,
+                                                    int32_t hv_segs, int32_t pull_seg) {
+  __shared__ int s_excl[kBlock / 32][32];
+  __shared__ int s_rs[kBlock / 32][32];
+  __shared__ int32_t s_aux[kBlock / 32][32];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  if (ctl->done) return;
+  const int wib = threadIdx.x >> 5;
+  if (ctl->mode == kModePush)
+    push_level(s_excl[wib], s_rs[wib], s_aux[wib], s_q[wib], row_ptr, col, wi, wf, is_float, ctl, q, segs, segcap,
+               inq, n, nwords);
+  else
+    pull_level(s_excl[wib], s_rs[wib], s_aux[wib], s_q[wib], row_ptr, t_row_ptr, t_col, t_wi, t_wf, is_float, ctl,
+               q, segs, segcap, inq, ul, ul_n, hv, hv_segoff, hv_count, hv_segs, pull_seg, n, nwords);
 }
 
 __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, int can_pull, cudaGraphConditionalHandle loop,
@@ -435,11 +456,9 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   a.in_graph = 0;
   void* clear_args[] = {&a.ctl, &a.inq, &a.n, &a.nwords, &a.inf};
   void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.last, &a.q, &a.segs, &a.inq, &a.n};
-  void* relax_args[] = {&a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.ctl, &a.q, &a.segs, &a.segcap,
-                        &a.inq, &a.n, &a.nwords};
-  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.t_wi, &a.t_wf, &a.is_float, &a.ctl, &a.q, &a.segs,
-                       &a.segcap, &a.inq, &a.ul, &a.ul_n, &a.hv, &a.hv_segoff, &a.hv_count, &a.hv_segs,
-                       &a.pull_seg, &a.n, &a.nwords};
+  void* step_args[] = {&a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.ctl, &a.q, &a.segs, &a.segcap,
+                       &a.inq, &a.n, &a.nwords, &a.t_row_ptr, &a.t_col, &a.t_wi, &a.t_wf, &a.ul, &a.ul_n, &a.hv,
+                       &a.hv_segoff, &a.hv_count, &a.hv_segs, &a.pull_seg};
   void* decide_args[] = {&a.ctl, &a.n, &a.can_pull, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
 
@@ -448,14 +467,11 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   fam.npre = 2;
   fam.pre[0] = {(const void*)sssp_clear, clear_args, dim3(sms * 4), dim3(kBlock)};
   fam.pre[1] = {(const void*)sssp_init, init_args, dim3(1), dim3(kBlock)};
-  fam.nbody = 3;
-  fam.body[0] = {(const void*)sssp_relax, relax_args,
-                 dim3(persistent_blocks((const void*)sssp_relax, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
-                 "sssp_relax", kModePush};
-  fam.body[1] = {(const void*)sssp_pull, pull_args,
-                 dim3(persistent_blocks((const void*)sssp_pull, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
-                 "sssp_pull", kModePull};
-  fam.body[2] = {(const void*)sssp_decide, decide_args, dim3(1), dim3(32), "sssp_decide"};
+  fam.nbody = 2;
+  fam.body[0] = {(const void*)sssp_step, step_args,
+                 dim3(persistent_blocks((const void*)sssp_step, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
+                 "sssp_step"};
+  fam.body[1] = {(const void*)sssp_decide, decide_args, dim3(1), dim3(32), "sssp_decide"};
   fam.npost = 1;
   fam.post[0] = {(const void*)sssp_next, next_args, dim3(1), dim3(32), "sssp_next"};
   fam.ctl = a.ctl;

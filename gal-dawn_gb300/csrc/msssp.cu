@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(1024) mw_init(MwCtl* __restrict__ ctl, const i
 
 // One level.  Warp tasks: the long-row segments, then the short-row
 // vertices of the input queue (grid-stride over warps).
-__global__ void __launch_bounds__(kBlock) mw_push(const int32_t* __restrict__ row_ptr,
+__global__ void __launch_bounds__(kBlock, 5) mw_push(const int32_t* __restrict__ row_ptr,
                                                   const int32_t* __restrict__ col, const int32_t* __restrict__ w,
                                                   int is_float, MwCtl* __restrict__ ctl, int32_t* __restrict__ D,
                                                   unsigned long long* __restrict__ masks, int32_t* __restrict__ q,
