@@ -55,10 +55,10 @@ def dist_env():
     return ws, rank, local
 
 
-def make_workload(scale, rank):
+def make_workload(scale, rank, weighted=False):
     from dawn_gb300 import gen
     t = time.time()
-    g = gen.rmat(scale, EDGEFACTOR, A, B, C, seed=GRAPH_SEED)
+    g = gen.rmat(scale, EDGEFACTOR, A, B, C, seed=GRAPH_SEED, weights=weighted)
     srcs = gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
     log(f"[bench] rmat{scale}: n={g.n} m={g.m} generated in {time.time() - t:.1f}s")
     return g, srcs
@@ -394,7 +394,8 @@ def main():
     ap.add_argument("--traced", action="store_true",
                     help="with --quick: run the steps level by level, launching only the kernels each level uses")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner before the timed steps")
-    ap.add_argument("--variant", default="bitset", choices=["bitset", "learned", "do", "push"])
+    ap.add_argument("--variant", default="bitset", choices=["bitset", "learned", "do", "push", "sssp", "sssp-single"],
+                    help="--quick only: the traversal to run (sssp: batched weighted, int32 weights)")
     ap.add_argument("--suite", action="store_true",
                     help="also time the other workload shapes (one JSON line each, before the main line)")
     args = ap.parse_args()
@@ -415,7 +416,7 @@ def main():
         _s = torch.cuda.Stream()
         torch.cuda.set_stream(_s)
         suite_lines(torch, abi, _gen, _s.cuda_stream, rank)
-    g, srcs = make_workload(args.scale, rank)
+    g, srcs = make_workload(args.scale, rank, weighted=args.quick and args.variant.startswith("sssp"))
     # A dedicated stream: the library launches on it and torch's events
     # record on it (the legacy default stream has handle 0, which the C ABI
     # reads as "library-owned stream").
@@ -427,13 +428,33 @@ def main():
     dg = abi.Graph(g, stream=stream)
     d_dist = torch.empty((NSRC, g.n), dtype=torch.int32, device="cuda")
     if args.quick:
-        var = {"bitset": abi.VARIANT_BITSET, "learned": abi.VARIANT_LEARNED, "do": abi.VARIANT_DO,
-               "push": abi.VARIANT_PUSH}[args.variant]
+        # Profiling form: the same traversal as a bench step (handle tuned
+        # first, untimed), with the measured steps inside an NVTX range
+        # "dawn-step" so a profiler can keep to exactly those launches.
+        if args.variant.startswith("sssp"):
+            dg.close()
+            dg = abi.Graph(g, weights="i32", stream=stream)
+            var = abi.VARIANT_AUTO if args.variant == "sssp" else abi.VARIANT_DO
+            run = lambda st=False: dg.sssp_device(srcs, d_dist.data_ptr(), variant=var, stats=st)  # noqa: E731
+        else:
+            var = {"bitset": abi.VARIANT_BITSET, "learned": abi.VARIANT_LEARNED, "do": abi.VARIANT_DO,
+                   "push": abi.VARIANT_PUSH}[args.variant]
+            if not args.no_tune and var in (abi.VARIANT_BITSET, abi.VARIANT_LEARNED):
+                dg.autotune(srcs)
+            run = lambda st=False: dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=st)  # noqa: E731
+        for _ in range(args.warmup):
+            run()
+        torch.cuda.synchronize()
         dg.trace(args.traced)
-        quick = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=False)  # noqa: E731
-        ms = time_steps(torch, quick, args.steps, args.warmup, barrier) / max(1, args.steps)
+
+        def quick():
+            torch.cuda.nvtx.range_push("dawn-step")
+            run()
+            torch.cuda.nvtx.range_pop()
+        ms = time_steps(torch, quick, args.steps, 0, barrier) / max(1, args.steps)
         recs = dg.trace_read() if args.traced else []
-        st = dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=True)
+        dg.trace(False)
+        st = run(True)
         if rank == 0:
             print(json.dumps({"quick": True, "variant": args.variant, "traced": args.traced, "scale": args.scale,
                               "ms_per_step": round(ms, 4), "edges": st.edges_traversed,

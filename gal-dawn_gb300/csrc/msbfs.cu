@@ -347,7 +347,7 @@ struct LevelAcc {
 // OR-ed into per-lane shared-memory slots.  The list is filtered into the
 // next unfinished list as it goes.
 template <int W>
-__global__ void __launch_bounds__(kBlock, 4) bs_pull(const int32_t* __restrict__ row_ptr,
+__global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t* __restrict__ row_ptr,
                                                      const int32_t* __restrict__ t_row_ptr,
                                                      const int32_t* __restrict__ t_col, BsCtl* __restrict__ ctl,
                                                      u64* __restrict__ visit, u64* __restrict__ fr,
