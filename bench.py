@@ -167,7 +167,7 @@ def bitset_roofline(dg, g, srcs, d_dist, abi, peak_gbs, peak_kind):
     return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak_gbs,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
             "traffic": int(traffic) if traffic else None,
-            "traffic_source": "profiles/bitset_bfs_rmat22_kernels.md (ncu dram__bytes_read.sum + "
+            "traffic_source": "profiles/learned_bfs_rmat22_kernels.md (ncu dram__bytes_read.sum + "
                               "dram__bytes_write.sum, per launch)" if traffic else None,
             "launches_per_step": k["launches"], "avg_launch_ms": round(avg_ms, 4),
             "alg_bytes_per_launch": int(avg_bytes), "kernel_share": share,
@@ -176,9 +176,9 @@ def bitset_roofline(dg, g, srcs, d_dist, abi, peak_gbs, peak_kind):
 
 def profiled_traffic(kernel, scale):
     """Per-launch DRAM bytes of `kernel` from the committed ncu summary of
-    this workload (profiles/bitset_bfs_rmat22_kernels.md), or None."""
+    this workload (profiles/learned_bfs_rmat22_kernels.md), or None."""
     import re
-    p = os.path.join(ROOT, "profiles", "bitset_bfs_rmat22_kernels.md")
+    p = os.path.join(ROOT, "profiles", "learned_bfs_rmat22_kernels.md")
     if scale != 22 or not os.path.exists(p):
         return None
     m = re.search(kernel + r" DRAM traffic per launch, averaged over the step's \d+ launches: ([0-9.]+) MB",
