@@ -18,6 +18,9 @@
 // without a value uses weight 1.
 #include <dawn/io.hxx>
 
+#include <sys/stat.h>
+
+#include <cstdlib>
 #include <parallel/algorithm>
 #include <tuple>
 
@@ -178,7 +181,109 @@ void build(DAWN::Graph::Graph_t& graph, std::vector<Entry>& e, bool symmetric, b
   graph.coo.val = nullptr;
 }
 
+// --- binary CSR cache -----------------------------------------------------
+//
+// Parsing a large MatrixMarket file dominates a tool's run time; the CSR it
+// yields depends only on the file and on the reader (symmetric or directed,
+// weighted or not).  With DAWN_CSR_CACHE set, the CSR is stored after the
+// first parse as <file name>.<s|d><w|u>.dawncsr, beside the input file
+// (DAWN_CSR_CACHE=1) or in the directory the variable names, together with
+// the input's size and modification time; a later load of the same,
+// unchanged file with the same reader reads the arrays back instead.  A
+// cache that does not match (other file, changed file, other reader, short
+// or damaged) is ignored and rewritten.
+
+struct CacheHeader {
+  char magic[8];
+  uint32_t version, flags;  // flags: 1 symmetric, 2 weighted
+  int64_t src_size, src_mtime_ns;
+  int32_t rows, pad;
+  int64_t nnz;
+};
+constexpr char kCacheMagic[8] = {'D', 'A', 'W', 'N', 'C', 'S', 'R', '1'};
+
+std::string cache_path(const std::string& input, bool symmetric, bool weighted) {
+  const char* env = std::getenv("DAWN_CSR_CACHE");
+  if (!env || !*env || std::string(env) == "0") return "";
+  std::string name = input;
+  std::string dir;
+  if (std::string(env) != "1") {
+    const size_t slash = input.find_last_of('/');
+    name = slash == std::string::npos ? input : input.substr(slash + 1);
+    dir = std::string(env) + "/";
+  }
+  return dir + name + "." + (symmetric ? "s" : "d") + (weighted ? "w" : "u") + ".dawncsr";
+}
+
+bool source_stat(const std::string& input, int64_t* size, int64_t* mtime_ns) {
+  struct stat st;
+  if (stat(input.c_str(), &st) != 0) return false;
+  *size = (int64_t)st.st_size;
+  *mtime_ns = (int64_t)st.st_mtim.tv_sec * 1000000000LL + (int64_t)st.st_mtim.tv_nsec;
+  return true;
+}
+
+bool load_cache(const std::string& cpath, const std::string& input, DAWN::Graph::Graph_t& graph, bool symmetric,
+                bool weighted) {
+  int64_t size = 0, mtime = 0;
+  if (!source_stat(input, &size, &mtime)) return false;
+  FILE* f = std::fopen(cpath.c_str(), "rb");
+  if (!f) return false;
+  CacheHeader h;
+  bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kCacheMagic, 8) == 0 && h.version == 1 &&
+            h.flags == (uint32_t)((symmetric ? 1 : 0) | (weighted ? 2 : 0)) && h.src_size == size &&
+            h.src_mtime_ns == mtime && h.rows == graph.rows && h.nnz >= 0 && h.nnz <= INT32_MAX;
+  if (ok) {
+    const int nnz = (int)h.nnz;
+    int* rp = new int[graph.rows + 1];
+    int* col = new int[nnz > 0 ? nnz : 1];
+    float* val = weighted ? new float[nnz > 0 ? nnz : 1] : nullptr;
+    ok = std::fread(rp, sizeof(int), (size_t)graph.rows + 1, f) == (size_t)graph.rows + 1 &&
+         std::fread(col, sizeof(int), (size_t)nnz, f) == (size_t)nnz &&
+         (!weighted || std::fread(val, sizeof(float), (size_t)nnz, f) == (size_t)nnz) && rp[0] == 0 &&
+         rp[graph.rows] == nnz;
+    if (ok) {
+      graph.nnz = (uint64_t)nnz;
+      graph.csr.row_ptr = rp;
+      graph.csr.col = col;
+      graph.csr.val = val;
+    } else {
+      delete[] rp;
+      delete[] col;
+      delete[] val;
+    }
+  }
+  std::fclose(f);
+  return ok;
+}
+
+void store_cache(const std::string& cpath, const std::string& input, const DAWN::Graph::Graph_t& graph,
+                 bool symmetric, bool weighted) {
+  CacheHeader h = {};
+  std::memcpy(h.magic, kCacheMagic, 8);
+  h.version = 1;
+  h.flags = (symmetric ? 1 : 0) | (weighted ? 2 : 0);
+  if (!source_stat(input, &h.src_size, &h.src_mtime_ns)) return;
+  h.rows = graph.rows;
+  h.nnz = (int64_t)graph.nnz;
+  const std::string tmp = cpath + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "wb");
+  if (!f) return;  // no cache (read-only directory, say): the load itself succeeded
+  const size_t nnz = (size_t)graph.nnz;
+  bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+            std::fwrite(graph.csr.row_ptr, sizeof(int), (size_t)graph.rows + 1, f) == (size_t)graph.rows + 1 &&
+            std::fwrite(graph.csr.col, sizeof(int), nnz, f) == nnz &&
+            (!weighted || std::fwrite(graph.csr.val, sizeof(float), nnz, f) == nnz);
+  ok = std::fclose(f) == 0 && ok;
+  if (ok)
+    std::rename(tmp.c_str(), cpath.c_str());
+  else
+    std::remove(tmp.c_str());
+}
+
 void read_any(std::string& input_path, DAWN::Graph::Graph_t& graph, bool symmetric, bool weighted) {
+  const std::string cpath = cache_path(input_path, symmetric, weighted);
+  if (!cpath.empty() && load_cache(cpath, input_path, graph, symmetric, weighted)) return;
   std::string text;
   if (!read_all(input_path, &text)) {
     std::cerr << "Error opening file " << input_path << std::endl;
@@ -186,6 +291,7 @@ void read_any(std::string& input_path, DAWN::Graph::Graph_t& graph, bool symmetr
   }
   std::vector<Entry> e = parse_entries(text, weighted, graph.rows, input_path);
   build(graph, e, symmetric, weighted);
+  if (!cpath.empty()) store_cache(cpath, input_path, graph, symmetric, weighted);
 }
 
 }  // namespace
@@ -222,21 +328,52 @@ void readList(std::string& input_path, DAWN::Graph::Graph_t& graph) {
 
 namespace {
 
-// Buffered text writer: the bytes of `ofstream << ... << std::endl` lines,
-// without a flush per line.
-struct Writer {
-  FILE* f;
-  std::vector<char> buf;
-  explicit Writer(FILE* file) : f(file) { buf.reserve(1 << 20); }
-  void put(const char* s, int k) {
-    buf.insert(buf.end(), s, s + k);
-    if (buf.size() > (1u << 20)) flush();
+// Text output: lines are formatted in parallel chunks (each thread fills its
+// own buffer) and written in order, in rounds that bound the memory held.
+// fmt(j, line) writes line j into `line` and returns its length (0: no line).
+template <class Fmt>
+void write_lines(FILE* f, int n, Fmt&& fmt) {
+  constexpr int kChunk = 1 << 15;
+  int nt = 1;
+#ifdef _OPENMP
+  nt = omp_get_max_threads();
+#endif
+  const int nchunks = (n + kChunk - 1) / kChunk;
+  const int round = 4 * nt;
+  std::vector<std::string> bufs((size_t)round);
+  for (int c0 = 0; c0 < nchunks; c0 += round) {
+    const int cn = std::min(round, nchunks - c0);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int b = 0; b < cn; b++) {
+      std::string& s = bufs[(size_t)b];
+      s.clear();
+      char line[128];
+      const int j0 = (c0 + b) * kChunk, j1 = std::min(n, j0 + kChunk);
+      for (int j = j0; j < j1; j++) {
+        const int k = fmt(j, line);
+        if (k > 0) s.append(line, (size_t)k);
+      }
+    }
+    for (int b = 0; b < cn; b++) std::fwrite(bufs[(size_t)b].data(), 1, bufs[(size_t)b].size(), f);
   }
-  void flush() {
-    if (!buf.empty()) std::fwrite(buf.data(), 1, buf.size(), f);
-    buf.clear();
+}
+
+// printf's %d, digit for digit.
+inline char* put_int(char* p, int v) {
+  uint32_t u = (uint32_t)v;
+  if (v < 0) {
+    *p++ = '-';
+    u = 0u - u;
   }
-};
+  char tmp[10];
+  int k = 0;
+  do {
+    tmp[k++] = (char)('0' + u % 10);
+    u /= 10;
+  } while (u);
+  while (k) *p++ = tmp[--k];
+  return p;
+}
 
 FILE* open_out(const std::string& path) {
   FILE* f = std::fopen(path.c_str(), "w");
@@ -250,11 +387,16 @@ void outfile(int n, int* result, int source, std::string& output_path) {
   FILE* f = open_out(output_path);
   if (!f) return;
   std::cout << "Start outfile" << std::endl;
-  Writer w(f);
-  char line[64];
-  for (int j = 0; j < n; j++)
-    if (source != j && result[j] > 0) w.put(line, std::snprintf(line, sizeof(line), "%d %d %d\n", source, j, result[j]));
-  w.flush();
+  write_lines(f, n, [&](int j, char* line) -> int {
+    if (source == j || result[j] <= 0) return 0;
+    char* p = put_int(line, source);
+    *p++ = ' ';
+    p = put_int(p, j);
+    *p++ = ' ';
+    p = put_int(p, result[j]);
+    *p++ = '\n';
+    return (int)(p - line);
+  });
   std::cout << "End outfile" << std::endl;
   std::fclose(f);
 }
@@ -264,12 +406,10 @@ void outfile(int n, float* result, int source, std::string& output_path) {
   FILE* f = open_out(output_path);
   if (!f) return;
   std::cout << "Start outfile" << std::endl;
-  Writer w(f);
-  char line[96];
-  for (int j = 0; j < n; j++)
-    if (source != j && result[j] != 0)
-      w.put(line, std::snprintf(line, sizeof(line), "%d %d %g\n", source, j, (double)result[j]));
-  w.flush();
+  write_lines(f, n, [&](int j, char* line) -> int {
+    if (source == j || result[j] == 0) return 0;
+    return std::snprintf(line, 128, "%d %d %g\n", source, j, (double)result[j]);
+  });
   std::cout << "End outfile" << std::endl;
   std::fclose(f);
 }
@@ -278,11 +418,14 @@ void outfile(int n, int* result, std::string& output_path) {
   FILE* f = open_out(output_path);
   if (!f) return;
   std::cout << "Start outfile" << std::endl;
-  Writer w(f);
-  char line[64];
-  for (int j = 0; j < n; j++)
-    if (result[j] > 0) w.put(line, std::snprintf(line, sizeof(line), "%d %d\n", j, result[j]));
-  w.flush();
+  write_lines(f, n, [&](int j, char* line) -> int {
+    if (result[j] <= 0) return 0;
+    char* p = put_int(line, j);
+    *p++ = ' ';
+    p = put_int(p, result[j]);
+    *p++ = '\n';
+    return (int)(p - line);
+  });
   std::cout << "End outfile" << std::endl;
   std::fclose(f);
 }
@@ -291,11 +434,10 @@ void outfile(int n, float* result, std::string& output_path) {
   FILE* f = open_out(output_path);
   if (!f) return;
   std::cout << "Start outfile" << std::endl;
-  Writer w(f);
-  char line[96];
-  for (int j = 0; j < n; j++)
-    if (result[j] != 0) w.put(line, std::snprintf(line, sizeof(line), "%d %.6f\n", j, (double)result[j]));
-  w.flush();
+  write_lines(f, n, [&](int j, char* line) -> int {
+    if (result[j] == 0) return 0;
+    return std::snprintf(line, 128, "%d %.6f\n", j, (double)result[j]);
+  });
   std::cout << "End outfile" << std::endl;
   std::fclose(f);
 }

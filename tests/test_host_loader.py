@@ -69,3 +69,80 @@ def test_reference_mains_build_against_this_api(tool, tmp_path):
                         "-I", INCLUDE_DIR, "-fopenmp", "-o", exe, "-L", LIB_DIR, "-ldawn_host", "-ldawn_gb300",
                         "-Wl,-rpath," + LIB_DIR], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     assert r.returncode == 0, r.stdout
+
+
+def test_csr_cache(goldens, tmp_path):
+    # DAWN_CSR_CACHE: the first load parses and stores the CSR; an unchanged
+    # file loads from the cache; a changed or damaged one is parsed again
+    import shutil
+    import time
+    cache = tmp_path / "cache"
+    cache.mkdir()
+    env = dict(os.environ, DAWN_CSR_CACHE=str(cache))
+    for g in goldens:
+        mtx = tmp_path / os.path.basename(g.mtx)
+        shutil.copy(g.mtx, mtx)
+
+        def load():
+            out = str(tmp_path / "csr.bin")
+            r = subprocess.run([os.path.join(BIN_DIR, "dump_csr"), str(mtx), str(int(g.weighted)), "0", out],
+                               stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, env=env)
+            assert r.returncode == 0, r.stdout
+            with open(out, "rb") as f:
+                rows, _ = np.frombuffer(f.read(8), np.int32)
+                nnz = int(np.frombuffer(f.read(8), np.int64)[0])
+                f.read(8)
+                rp = np.frombuffer(f.read(4 * (rows + 1)), np.int32)
+                col = np.frombuffer(f.read(4 * nnz), np.int32)
+                val = np.frombuffer(f.read(4 * nnz), np.float32) if g.weighted else None
+            assert np.array_equal(rp, g.row_ptr) and np.array_equal(col, g.col), g.name
+            if g.weighted:
+                assert np.array_equal(val, g.w_f32), g.name
+            files = list(cache.glob(mtx.name + ".*.dawncsr"))
+            assert len(files) == 1, files
+            return files[0], files[0].stat().st_mtime_ns
+
+        path, t1 = load()
+        assert (".d" if g.directed else ".s") in path.name
+        _, t2 = load()
+        assert t2 == t1  # read back, not rewritten
+        st = mtx.stat()
+        os.utime(mtx, ns=(st.st_atime_ns, st.st_mtime_ns + 1_000_000_000))
+        time.sleep(0.01)
+        _, t3 = load()
+        assert t3 != t2  # the changed file was parsed again
+        with open(path, "r+b") as f:
+            f.truncate(40)
+        _, t4 = load()
+        assert t4 != t3 and path.stat().st_size > 40
+
+
+def test_outfile_text_matches_printf(tmp_path):
+    # the parallel writer produces the bytes of the printf formats the
+    # reference's ostream output amounts to (%d, %g, %.6f)
+    exe = str(tmp_path / "outfile_check")
+    src = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cpp", "outfile_check.cpp")
+    r = subprocess.run(["g++", "-std=c++17", src, "-I", os.path.join(HOST_DIR, "include"), "-I", INCLUDE_DIR,
+                        "-fopenmp", "-o", exe, "-L", LIB_DIR, "-ldawn_host", "-ldawn_gb300",
+                        "-Wl,-rpath," + LIB_DIR], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert r.returncode == 0, r.stdout
+    rng = np.random.default_rng(3)
+    n, source = 200_000, 777
+    iv = rng.integers(-5, 1 << 20, n).astype(np.int32)
+    iv[:6] = [0, -1, 2**31 - 1, -2**31, 1, 10**9]
+    fv = (rng.standard_normal(n) * 10.0 ** rng.integers(-8, 9, n)).astype(np.float32)
+    fv[:7] = [0.0, np.float32(3.4028235e38), np.float32(1e-40), -0.0, 1.0, np.float32(123456.78), np.nan]
+    fv[rng.integers(0, n, 5000)] = 0.0
+    inp = tmp_path / "vals.bin"
+    with open(inp, "wb") as f:
+        f.write(np.array([n, source], np.int32).tobytes() + iv.tobytes() + fv.tobytes())
+    r = subprocess.run([exe, str(inp), str(tmp_path / "out")], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       text=True)
+    assert r.returncode == 0, r.stdout
+    want_is = "".join("%d %d %d\n" % (source, j, v) for j, v in enumerate(iv.tolist()) if j != source and v > 0)
+    want_fs = "".join("%d %d %g\n" % (source, j, v) for j, v in enumerate(fv.tolist()) if j != source and v != 0)
+    want_i = "".join("%d %d\n" % (j, v) for j, v in enumerate(iv.tolist()) if v > 0)
+    want_f = "".join("%d %.6f\n" % (j, v) for j, v in enumerate(fv.tolist()) if v != 0)
+    for ext, want in ((".is", want_is), (".fs", want_fs), (".i", want_i), (".f", want_f)):
+        got = (tmp_path / ("out" + ext)).read_text()
+        assert got == want, ext
