@@ -140,7 +140,7 @@ void destroy(dawn_graph* g) {
                     &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
                     &g->dist_stage, &g->pt_voff, &g->pt_tasks, &g->pt_sources, &g->pt_ctl, &g->pt_scratch, &g->pt_rows,
                     &g->sel_slot, &g->wt_col, &g->wt_val, &g->mw_block, &g->mw_masks,
-                    &g->mw_ctl, &g->mw_sources};
+                    &g->mw_ctl, &g->mw_sources, &g->bc_levels, &g->bc_terms, &g->bc_range, &g->bc_out};
   for (DevBuf* b : bufs) dawn::release(*b);
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);
@@ -611,6 +611,37 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources, int32_t nsrc, 
   }
   dawn::release(srcbuf);
   return s;
+}
+
+dawn_status dawn_betweenness_device(dawn_graph* g, const int32_t* sources, int32_t nsrc, double* d_bc,
+                                    dawn_stats* stats) {
+  dawn::clear_error();
+  if (!g || !d_bc) {
+    dawn::set_error("graph or output is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  DAWN_CHECK(check_sources(g, sources, nsrc));
+  if (stats) DAWN_CUDA(cudaEventRecord(g->ev0, g->stream));
+  DAWN_CHECK(dawn::betweenness(g, sources, nsrc, d_bc, stats));
+  if (stats) {
+    DAWN_CUDA(cudaEventRecord(g->ev1, g->stream));
+    DAWN_CUDA(cudaEventSynchronize(g->ev1));
+    DAWN_CUDA(cudaEventElapsedTime(&stats->device_ms, g->ev0, g->ev1));
+  }
+  return DAWN_OK;
+}
+
+dawn_status dawn_betweenness(dawn_graph* g, const int32_t* sources, int32_t nsrc, double* bc, dawn_stats* stats) {
+  dawn::clear_error();
+  if (!g || !bc) {
+    dawn::set_error("graph or output is NULL");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  DAWN_CHECK(dawn::ensure(g->bc_out, sizeof(double) * (size_t)g->n, g->stream));
+  DAWN_CHECK(dawn_betweenness_device(g, sources, nsrc, g->bc_out.as<double>(), stats));
+  DAWN_CUDA(cudaMemcpyAsync(bc, g->bc_out.p, sizeof(double) * (size_t)g->n, cudaMemcpyDeviceToHost, g->stream));
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  return DAWN_OK;
 }
 
 dawn_status dawn_graph_set_parts(dawn_graph* g, int32_t nparts, const int32_t* offsets) {

@@ -178,6 +178,10 @@ struct dawn_graph {
   dawn::DevBuf ss_ctl;      // SsCtl
   dawn::DevBuf ss_sources;  // int32 source list of the current call
   dawn::DevBuf ss_scratch;  // n x u64 (GOVM source-row resolution)
+  dawn::DevBuf bc_levels;   // betweenness: n x 64 int32 levels of a batch
+  dawn::DevBuf bc_terms;    // n x 64 float (1 / amount + dependency)
+  dawn::DevBuf bc_range;    // 2 x n int32 lowest / highest level per vertex
+  dawn::DevBuf bc_out;      // n double (host-pointer calls)
   dawn::DevBuf mw_block;    // batched weighted traversal: n x 64 int32 distances
   dawn::DevBuf mw_masks;    // 3 x n uint64 improved-source masks
   dawn::DevBuf mw_ctl;
@@ -267,6 +271,9 @@ dawn_status tune_cache_load(const char* path);
 dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, void* d_dist);
 dawn_status sssp_batched_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc);
 
+// bc.cu: BCDAWN betweenness summed over the sources into d_bc (n doubles).
+dawn_status betweenness(dawn_graph* g, const int32_t* sources, int32_t nsrc, double* d_bc, dawn_stats* st);
+
 // parts.cu
 dawn_status parts_set(dawn_graph* g, int32_t nparts, const int32_t* offsets);
 dawn_status parts_bfs(dawn_graph* g, const int32_t* source_offset,
@@ -287,6 +294,11 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                        int32_t* d_dist, unsigned long long* cc_sum = nullptr,
                        unsigned long long* cc_cnt = nullptr);
 dawn_status bfs_bitset_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc);
+// One batch of at most 64 sources: levels as n x 64 int32 rows (vertex-major,
+// -1 unreached), per vertex the lowest and highest level (2 x n int32), and
+// the deepest level reached.
+dawn_status bfs_bitset_levels(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_levels,
+                              int32_t* d_range, int32_t* deepest);
 int bitset_width(const dawn_graph* g, int32_t nsrc);
 // govm.cu
 dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,

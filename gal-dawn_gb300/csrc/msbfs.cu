@@ -56,6 +56,8 @@ struct BsCtl {
   unsigned long long full[kMaxW];  // this batch's source bits
   int32_t* dist_base;
   const int32_t* sources;
+  int32_t* lv_block;            // level mode: n x 64 levels, vertex-major (else NULL)
+  int32_t* lv_range;            // level mode: per vertex, lowest and highest level reached
   unsigned long long* cc_sum;   // closeness mode: per source, sum of hop distances (else NULL)
   unsigned long long* cc_cnt;   // closeness mode: per source, vertices reached besides itself
   int32_t use_sel;              // decide with the handle's selector weights
@@ -786,9 +788,46 @@ __device__ __forceinline__ void emit_closeness(const BsCtl* __restrict__ ctl, co
   }
 }
 
+// Level mode of the final pass (one-word batches): each vertex's levels for
+// the batch's sources as one 64-word row (-1 where unreached), and the
+// lowest and highest level among them (INT_MAX / -1 when none).
+template <int W>
+__device__ __forceinline__ void emit_levels(const BsCtl* __restrict__ ctl, const u64* __restrict__ visit,
+                                            const u64* __restrict__ slices, int32_t n, int nb, int nbits) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < (size_t)n; u += stride) {
+    const u64 vis = visit[u * W];
+    int lo = 0x7fffffff, hi = -1;
+    int4* row = reinterpret_cast<int4*>(ctl->lv_block + u * 64);
+    for (int s0 = 0; s0 < 64; s0 += 4) {
+      int32_t v[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const int s = s0 + j;
+        v[j] = -1;
+        if (s < nb && ((vis >> s) & 1ull)) {
+          int32_t x = 0;
+          for (int k = 0; k < nbits; k++) x |= (int32_t)((slices[((size_t)k * n + u) * W] >> s) & 1ull) << k;
+          v[j] = x;
+          lo = min(lo, x);
+          hi = max(hi, x);
+        }
+      }
+      row[s0 / 4] = make_int4(v[0], v[1], v[2], v[3]);
+    }
+    ctl->lv_range[2 * u] = lo;
+    ctl->lv_range[2 * u + 1] = hi;
+  }
+}
+
 template <int W>
 __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__ ctl, const u64* __restrict__ visit,
                                                        const u64* __restrict__ slices, int32_t n) {
+  if (ctl->lv_block) {
+    if (W == 1)
+      emit_levels<W>(ctl, visit, slices, n, min(64, ctl->nsrc - ctl->batch * 64), 32 - __clz(max(ctl->level, 1)));
+    return;
+  }
   if (ctl->cc_sum) {
     const int per = 64 * W;
     emit_closeness<W>(ctl, visit, slices, n, min(per, ctl->nsrc - ctl->batch * per),
@@ -1003,7 +1042,8 @@ namespace {
 
 template <int W>
 dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_dist,
-                      unsigned long long* cc_sum, unsigned long long* cc_cnt) {
+                      unsigned long long* cc_sum, unsigned long long* cc_cnt, int32_t* lv_block = nullptr,
+                      int32_t* lv_range = nullptr) {
   const int32_t n = g->n;
   const size_t nn = (size_t)n;
   const int wi = W == 1 ? 0 : (W == 2 ? 1 : 2);
@@ -1049,6 +1089,8 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   c.sources = g->bs_sources.as<int32_t>();
   c.cc_sum = cc_sum;
   c.cc_cnt = cc_cnt;
+  c.lv_block = lv_block;
+  c.lv_range = lv_range;
   c.use_sel = g->sel_call;
   c.sel_margin = g->sel_margin;
   c.force = g->force_variant;
@@ -1160,6 +1202,20 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   if (w == 4) return run_width<4>(g, sources, nsrc, d_dist, cc_sum, cc_cnt);
   if (w == 2) return run_width<2>(g, sources, nsrc, d_dist, cc_sum, cc_cnt);
   return run_width<1>(g, sources, nsrc, d_dist, cc_sum, cc_cnt);
+}
+
+dawn_status bfs_bitset_levels(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_levels,
+                              int32_t* d_range, int32_t* deepest) {
+  if (nsrc < 1 || nsrc > 64) {
+    set_error("level mode takes 1 to 64 sources per call");
+    return DAWN_ERR_INVALID_ARG;
+  }
+  DAWN_CHECK(run_width<1>(g, sources, nsrc, nullptr, nullptr, nullptr, d_levels, d_range));
+  BsCtl h;
+  DAWN_CUDA(cudaMemcpyAsync(&h, g->bs_ctl.p, sizeof(BsCtl), cudaMemcpyDeviceToHost, g->stream));
+  DAWN_CUDA(cudaStreamSynchronize(g->stream));
+  *deepest = h.level - 1;  // the batch ended on an empty level
+  return DAWN_OK;
 }
 
 dawn_status bfs_bitset_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc) {

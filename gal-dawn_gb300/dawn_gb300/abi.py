@@ -23,7 +23,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libdawn_gb300.so")
 # Every symbol the header declares; tests check the library exports them.
 EXPORTS = ("dawn_graph_create", "dawn_graph_create_device", "dawn_graph_destroy",
            "dawn_graph_set_stream", "dawn_graph_synchronize", "dawn_bfs", "dawn_bfs_device", "dawn_bfs_static",
-           "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_graph_set_option",
+           "dawn_sssp", "dawn_sssp_device", "dawn_closeness", "dawn_betweenness", "dawn_betweenness_device", "dawn_graph_set_option",
            "dawn_graph_get_option", "dawn_graph_set_selector", "dawn_autotune", "dawn_tune_cache_save",
            "dawn_tune_cache_load", "dawn_graph_set_parts", "dawn_multi_bfs", "dawn_multi_bfs_device",
            "dawn_multi_closeness", "dawn_trace_enable", "dawn_trace_read", "dawn_last_error", "dawn_version")
@@ -94,6 +94,8 @@ def lib():
                                      ctypes.POINTER(Stats)]
         L.dawn_graph_set_option.argtypes = [_VP, ctypes.c_int32, ctypes.c_int64]
         L.dawn_graph_get_option.argtypes = [_VP, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
+        L.dawn_betweenness.argtypes = [_VP, _VP, ctypes.c_int32, _VP, ctypes.POINTER(Stats)]
+        L.dawn_betweenness_device.argtypes = L.dawn_betweenness.argtypes
         L.dawn_graph_set_selector.argtypes = [_VP, _VP, ctypes.c_int32]
         L.dawn_autotune.argtypes = [_VP, _VP, ctypes.c_int32, ctypes.c_uint32, ctypes.POINTER(Tuning)]
         L.dawn_tune_cache_save.argtypes = [ctypes.c_char_p]
@@ -215,6 +217,15 @@ class Graph:
         _check(lib().dawn_autotune(self.handle, _ptr(s), len(s), TUNE_USE_CACHE if use_cache else 0,
                                    ctypes.byref(t)))
         return t.as_dict()
+
+    def betweenness(self, sources=None):
+        """dawn_betweenness over `sources` (default: every vertex, the
+        reference's BC_CPU::Betweenness_Centrality)."""
+        s = np.arange(self.n, dtype=np.int32) if sources is None else np.ascontiguousarray(sources, np.int32)
+        bc = np.empty(self.n, np.float64)
+        st = Stats()
+        _check(lib().dawn_betweenness(self.handle, _ptr(s), len(s), _ptr(bc), ctypes.byref(st)))
+        return bc, st
 
     def set_selector(self, weights):
         """dawn_graph_set_selector: load MLP weights (1475 floats) or None."""

@@ -140,6 +140,22 @@ dawn_status dawn_bfs_static(const int32_t* row_ptr, const int32_t* col,
                             int32_t n, int64_t m, int32_t source,
                             int32_t* dist, uint32_t flags, void* stream);
 
+/* BCDAWN betweenness: for each vertex, the sum over `sources` of the
+ * reference's dependency (src/algorithm/cpu/bc.cpp:9-191, the CPU-only
+ * BC_CPU::Betweenness_Centrality, which takes every vertex as a source).
+ * With levels counted from a source s, a vertex c at level >= 2 splits 1
+ * equally over its predecessor entries (CSR entries j -> c with level(j) =
+ * level(c) - 1, duplicates counted), and each predecessor also receives
+ * c's own dependency in full.  bc (host, n doubles) receives the sums;
+ * pass every vertex as a source for the reference's result.  The terms are
+ * float32 like the reference's; they agree with it to float rounding.
+ * Sources go 64 per batched traversal. */
+dawn_status dawn_betweenness(dawn_graph* g, const int32_t* sources,
+                             int32_t nsrc, double* bc, dawn_stats* stats);
+dawn_status dawn_betweenness_device(dawn_graph* g, const int32_t* sources,
+                                    int32_t nsrc, double* d_bc,
+                                    dawn_stats* stats);
+
 /* Many independent graphs in one call (no counterpart in the reference,
  * which traverses one graph per MSSP_GPU::run, src/algorithm/gpu/mssp.cu:9-51).
  * The handle's graph is declared the disjoint union of nparts graphs:

@@ -248,3 +248,127 @@ int oracle_num_threads(void) {
   return 1;
 #endif
 }
+
+/* --- BCDAWN betweenness (bc.cpp:9-191) --------------------------------------
+ * Per source s (BC_CPU::SOVM + kernel + accumulate):
+ *   * the first frontier is the set of s's out-neighbours (bc.cpp:57-62),
+ *     which are also marked visited; s itself is never marked;
+ *   * each step scans the frontier in vertex order and, for every CSR entry
+ *     j -> c whose head c is unvisited, counts amount[c]++ and records the
+ *     pair (j, c) (bc.cpp:126-140); then, pair by pair, c != s gets j
+ *     appended to its predecessor list, j gains 1 / amount[c], c joins the
+ *     next frontier and, the first time, the discovery order
+ *     (bc.cpp:142-158);
+ *   * finally, in reverse discovery order, every c adds its value to each of
+ *     its predecessors, in the order they were appended (bc.cpp:173-191).
+ * The result is the sum over the sources.  T selects the arithmetic: double
+ * for the oracle, float to repeat the reference's float32 additions in its
+ * order. */
+#define BC_SOURCE(T, NAME)                                                                   \
+  static void NAME(const int32_t* rp, const int32_t* col, int32_t n, int32_t s, T* delta,   \
+                   uint8_t* alpha, uint8_t* beta, uint8_t* gamma, int32_t* amount,          \
+                   int32_t* pj, int32_t* pc, int64_t* head, int64_t* tail, int64_t* nxt,    \
+                   int32_t* order) {                                                         \
+    memset(alpha, 0, (size_t)n);                                                             \
+    memset(beta, 0, (size_t)n);                                                              \
+    memset(gamma, 0, (size_t)n);                                                             \
+    memset(amount, 0, sizeof(int32_t) * (size_t)n);                                          \
+    for (int32_t v = 0; v < n; v++) head[v] = tail[v] = -1;                                  \
+    for (int32_t k = rp[s]; k < rp[s + 1]; k++) alpha[col[k]] = gamma[col[k]] = 1;           \
+    int64_t npairs_total = 0;                                                                \
+    int32_t norder = 0;                                                                      \
+    for (int32_t step = 1; step < n;) {                                                      \
+      step++;                                                                                \
+      uint8_t* in = (step % 2) ? beta : alpha;                                               \
+      uint8_t* out = (step % 2) ? alpha : beta;                                              \
+      int converged = 1;                                                                     \
+      int64_t p0 = npairs_total;                                                             \
+      for (int32_t j = 0; j < n; j++) {                                                      \
+        if (!in[j]) continue;                                                                \
+        for (int32_t k = rp[j]; k < rp[j + 1]; k++) {                                        \
+          const int32_t c = col[k];                                                          \
+          if (!gamma[c]) {                                                                   \
+            amount[c] += 1;                                                                  \
+            pj[npairs_total] = j;                                                            \
+            pc[npairs_total] = c;                                                            \
+            npairs_total++;                                                                  \
+            converged = 0;                                                                   \
+          }                                                                                  \
+        }                                                                                    \
+        in[j] = 0;                                                                           \
+      }                                                                                      \
+      for (int64_t p = p0; p < npairs_total; p++) {                                          \
+        const int32_t j = pj[p], c = pc[p];                                                  \
+        if (c == s || j == s) continue;                                                      \
+        nxt[p] = -1;                                                                         \
+        if (tail[c] < 0) head[c] = p; else nxt[tail[c]] = p;                                 \
+        tail[c] = p;                                                                         \
+        delta[j] += (T)1 / (T)amount[c];                                                     \
+        out[c] = 1;                                                                          \
+        if (!gamma[c]) {                                                                     \
+          gamma[c] = 1;                                                                      \
+          order[norder++] = c;                                                               \
+        }                                                                                    \
+      }                                                                                      \
+      if (converged) break;                                                                  \
+    }                                                                                        \
+    for (int32_t i = norder - 1; i >= 0; i--) {                                              \
+      const int32_t c = order[i];                                                            \
+      for (int64_t p = head[c]; p >= 0; p = nxt[p]) delta[pj[p]] += delta[c];               \
+    }                                                                                        \
+  }
+
+BC_SOURCE(double, bc_source_d)
+BC_SOURCE(float, bc_source_f)
+
+/* Betweenness summed over `sources`.  bc (double, may be NULL) from the
+ * double restatement, sources in parallel; bcf (float, may be NULL) with
+ * the reference's float32 arithmetic and order (sources in sequence, the
+ * per-source values added as bc_values[j] += bc_temp[j], bc.cpp:24-27). */
+void oracle_bc(const int32_t* rp, const int32_t* col, int32_t n, const int32_t* sources, int32_t nsrc,
+               double* bc, float* bcf) {
+  const int64_t m = rp[n];
+  if (bc) {
+    memset(bc, 0, sizeof(double) * (size_t)n);
+#pragma omp parallel
+    {
+      double* acc = (double*)calloc((size_t)n, sizeof(double));
+      double* delta = (double*)malloc(sizeof(double) * (size_t)n);
+      uint8_t* a = (uint8_t*)malloc((size_t)n * 3);
+      int32_t* amount = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+      int32_t* pj = (int32_t*)malloc(sizeof(int32_t) * (size_t)(m + 1));
+      int32_t* pc = (int32_t*)malloc(sizeof(int32_t) * (size_t)(m + 1));
+      int64_t* hd = (int64_t*)malloc(sizeof(int64_t) * (size_t)n * 2);
+      int64_t* nx = (int64_t*)malloc(sizeof(int64_t) * (size_t)(m + 1));
+      int32_t* order = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+#pragma omp for schedule(dynamic, 1)
+      for (int32_t i = 0; i < nsrc; i++) {
+        memset(delta, 0, sizeof(double) * (size_t)n);
+        bc_source_d(rp, col, n, sources[i], delta, a, a + n, a + 2 * (size_t)n, amount, pj, pc, hd, hd + n, nx,
+                    order);
+        for (int32_t v = 0; v < n; v++) acc[v] += delta[v];
+      }
+#pragma omp critical
+      for (int32_t v = 0; v < n; v++) bc[v] += acc[v];
+      free(acc); free(delta); free(a); free(amount); free(pj); free(pc); free(hd); free(nx); free(order);
+    }
+  }
+  if (bcf) {
+    memset(bcf, 0, sizeof(float) * (size_t)n);
+    float* delta = (float*)malloc(sizeof(float) * (size_t)n);
+    uint8_t* a = (uint8_t*)malloc((size_t)n * 3);
+    int32_t* amount = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    int32_t* pj = (int32_t*)malloc(sizeof(int32_t) * (size_t)(m + 1));
+    int32_t* pc = (int32_t*)malloc(sizeof(int32_t) * (size_t)(m + 1));
+    int64_t* hd = (int64_t*)malloc(sizeof(int64_t) * (size_t)n * 2);
+    int64_t* nx = (int64_t*)malloc(sizeof(int64_t) * (size_t)(m + 1));
+    int32_t* order = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+    for (int32_t i = 0; i < nsrc; i++) {
+      memset(delta, 0, sizeof(float) * (size_t)n);
+      bc_source_f(rp, col, n, sources[i], delta, a, a + n, a + 2 * (size_t)n, amount, pj, pc, hd, hd + n, nx,
+                  order);
+      for (int32_t v = 0; v < n; v++) bcf[v] += delta[v];
+    }
+    free(delta); free(a); free(amount); free(pj); free(pc); free(hd); free(nx); free(order);
+  }
+}

@@ -57,6 +57,8 @@ def port():
         L.oracle_sssp.restype = None
         L.oracle_mssp.argtypes = [_I, _I, ctypes.c_int32, _I, ctypes.c_int32,
                                   ctypes.c_int32, _I, _U8]
+        L.oracle_bc.argtypes = [_I, _I, ctypes.c_int32, _I, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_bc.restype = None
         L.oracle_mssp.restype = ctypes.c_int64
         L.oracle_msssp.argtypes = [_I, _I, _F, ctypes.c_int32, _I, ctypes.c_int32,
                                    ctypes.c_int32, _F]
@@ -87,6 +89,8 @@ def ref():
     if _ref is None:
         L = ctypes.CDLL(REF_LIB)
         L.ref_bfs_kernel.argtypes = [_I, _I, ctypes.c_int32, ctypes.c_int32, _I]
+        L.ref_bc.argtypes = [_I, _I, ctypes.c_int32, _F]
+        L.ref_bc.restype = None
         L.ref_bfs_bitmap.argtypes = [_I, _I, ctypes.c_int32, ctypes.c_int32, _I]
         L.ref_sssp.argtypes = [_I, _I, _F, ctypes.c_int32, ctypes.c_int32, _F]
         L.ref_cc.argtypes = [_I, _I, _F, ctypes.c_int32, ctypes.c_int32]
@@ -162,6 +166,21 @@ def closeness_ref_int(dist_ref_row, source):
     return port().oracle_closeness_ref_int(_ip(d), d.shape[0], int(source))
 
 
+def bc(g, sources=None, exact_ref_order=False):
+    """BCDAWN betweenness summed over `sources` (default: every vertex):
+    float64 restatement, or with exact_ref_order the reference's float32
+    arithmetic in its order."""
+    rp, col = _csr(g)
+    s = np.arange(g.n, dtype=np.int32) if sources is None else np.ascontiguousarray(sources, np.int32)
+    if exact_ref_order:
+        out = np.zeros(g.n, np.float32)
+        port().oracle_bc(_ip(rp), _ip(col), g.n, _ip(s), len(s), None, out.ctypes.data)
+    else:
+        out = np.zeros(g.n, np.float64)
+        port().oracle_bc(_ip(rp), _ip(col), g.n, _ip(s), len(s), out.ctypes.data, None)
+    return out
+
+
 def num_threads():
     return port().oracle_num_threads()
 
@@ -217,3 +236,11 @@ def ref_mssp(g, sources, want_dist=True):
     t = ref().ref_mssp_run(_ip(rp), _ip(col), None, g.n, g.m, _ip(s), len(s), 0,
                            _ip(d) if d is not None else None, None)
     return d, t
+
+
+def ref_bc(g):
+    """The reference's BC_CPU::Betweenness_Centrality (every vertex a source)."""
+    rp, col = _csr(g)
+    out = np.zeros(g.n, np.float32)
+    ref().ref_bc(_ip(rp), _ip(col), g.n, _fp(out))
+    return out

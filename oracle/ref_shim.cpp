@@ -1,13 +1,14 @@
 // ORACLE — test infrastructure only.
 //
 // C entry points around the reference's own, unmodified CPU algorithm files
-// (src/algorithm/cpu/{bfs,sssp,cc,mssp}.cpp, src/matrix.cpp, src/tool.cpp),
+// (src/algorithm/cpu/{bfs,sssp,cc,mssp,bc}.cpp, src/matrix.cpp, src/tool.cpp),
 // compiled from where they lie by oracle/Makefile into oracle/_ref/.  The
 // reference reports results only through DAWN::IO::outfile
 // (src/io.cpp:215-281); this file defines those four overloads to capture
 // the distance array instead of writing text, so the reference's results
 // can be compared in-process.
 
+#include <dawn/algorithm/cpu/bc.hxx>
 #include <dawn/algorithm/cpu/bfs.hxx>
 #include <dawn/algorithm/cpu/cc.hxx>
 #include <dawn/algorithm/cpu/mssp.hxx>
@@ -46,7 +47,9 @@ void outfile(int n, float* result, int source, std::string&) {
     std::memcpy(g_rows_f[source], result, sizeof(float) * (size_t)n);
 }
 void outfile(int, int*, std::string&) {}
-void outfile(int, float*, std::string&) {}
+void outfile(int n, float* result, std::string&) {
+  if (g_cap_f) std::memcpy(g_cap_f, result, sizeof(float) * (size_t)n);
+}
 }  // namespace IO
 }  // namespace DAWN
 
@@ -113,6 +116,23 @@ float ref_cc(const int32_t* row_ptr, const int32_t* col, const float* val,
   }
   return DAWN::CC_CPU::kernel(const_cast<int*>(row_ptr), const_cast<int*>(col),
                               n, source, t);
+}
+
+// BC_CPU::Betweenness_Centrality (bc.cpp:9-39): BCDAWN summed over every
+// vertex as a source, float32, as the reference's bc_cpu computes it.
+void ref_bc(const int32_t* row_ptr, const int32_t* col, int32_t n, float* bc) {
+  DAWN::Graph::Graph_t graph;
+  graph.rows = n;
+  graph.cols = n;
+  graph.nnz = (uint64_t)row_ptr[n];
+  graph.csr.row_ptr = const_cast<int*>(row_ptr);
+  graph.csr.col = const_cast<int*>(col);
+  std::string path;
+  g_cap_f = bc;
+  DAWN::BC_CPU::Betweenness_Centrality(graph, path);
+  g_cap_f = nullptr;
+  graph.csr.row_ptr = nullptr;
+  graph.csr.col = nullptr;
 }
 
 // MSSP_CPU::run (mssp.cpp:9-32) over a caller CSR.  With dist == NULL the

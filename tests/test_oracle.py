@@ -143,3 +143,37 @@ def test_port_matches_reference_with_duplicates_and_self_loops():
     for s in range(0, n, 37):
         assert np.array_equal(O.bfs_queue(g, s)[0], O.ref_bfs_kernel(g, s))
         assert np.array_equal(O.sssp(g, s), O.ref_sssp(g, s))
+
+
+def test_bc_hand_path():
+    # path 0-1-2 (both directions): sources 0 and 2 each credit vertex 1
+    # with 1 (its successor has one predecessor); source 1 credits nobody
+    g = Csr(3, [(0, 1), (1, 0), (1, 2), (2, 1)])
+    assert np.allclose(O.bc(g), [0.0, 2.0, 0.0])
+    assert O.bc(g, [0]).tolist() == [0.0, 1.0, 0.0]
+
+
+def test_bc_hand_diamond():
+    # 0 -> {1, 2} -> 3 -> 4 (directed): from 0, vertex 3 has two
+    # predecessors (1/2 each) and passes its own 1 (from 4) on undivided
+    g = Csr(5, [(0, 1), (0, 2), (1, 3), (2, 3), (3, 4)])
+    d = O.bc(g, [0])
+    assert np.allclose(d, [0.0, 1.5, 1.5, 1.0, 0.0])
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference not built here")
+def test_bc_port_matches_reference():
+    # the float32 restatement repeats the reference's bc_cpu bit for bit; the
+    # float64 one agrees to float32 rounding
+    graphs = [gen.rmat(8, 8, seed=81), gen.erdos_renyi(300, 1500, seed=82), gen.grid(9, 13),
+              gen.rmat(7, 4, seed=83)]
+    # duplicates and a self loop, as a hand-filled CSR may carry
+    rp = np.array([0, 3, 5, 7, 8], np.int32)
+    col = np.array([1, 1, 2, 0, 3, 3, 2, 3], np.int32)
+    graphs.append(gen.CsrGraph(4, rp, col))
+    for g in graphs:
+        want = O.ref_bc(g)
+        got = O.bc(g, exact_ref_order=True)
+        assert np.array_equal(got, want), g.n
+        d = O.bc(g)
+        np.testing.assert_allclose(d, want.astype(np.float64), rtol=1e-5, atol=1e-4)
