@@ -361,6 +361,16 @@ def suite_lines(torch, abi, gen, stream, rank):
                     "sources": int(sum(len(x) for x in gsrcs)), "n_total": u.n, "m_total": u.m,
                     "levels": st.levels, "tasks": st.batches})
     del u, d
+    # BCDAWN betweenness of every vertex, RMAT scale 16 (65,536 sources)
+    gb = gen.rmat(16, EDGEFACTOR, A, B, C, seed=GRAPH_SEED)
+    with abi.Graph(gb, stream=stream) as dg:
+        dg.betweenness(np.arange(64, dtype=np.int32))
+        t0 = time.perf_counter()
+        _, st = dg.betweenness()
+        wall = time.perf_counter() - t0
+        out.append({"suite": "rmat16-betweenness-all-vertices", "sources": gb.n, "n": gb.n, "m": gb.m,
+                    "device_ms": round(st.device_ms, 2), "wall_ms": round(wall * 1e3, 2),
+                    "sources_per_s": round(gb.n / wall, 1), "batches": st.batches})
     # the same graphs one at a time (first 32): batched bitset per graph, and
     # the plain single-source traversal per (graph, source)
     sub = 32

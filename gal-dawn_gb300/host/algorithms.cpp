@@ -6,6 +6,7 @@
 // dawn_* call on the GB300 kernels.  The graph is uploaded once per run()
 // (the reference copies it once per source, see bfs.cuh:14-19).
 #include <dawn/algorithm/gpu/apsp.cuh>
+#include <dawn/algorithm/gpu/bc.cuh>
 #include <dawn/algorithm/gpu/cc.cuh>
 #include <dawn/algorithm/gpu/mssp.cuh>
 
@@ -228,6 +229,19 @@ double CC_GPU::closeness(Graph::Graph_t& graph, int source, bool is_weighted) {
   dawn_status s = dawn_closeness(dev.g, &source, 1, is_weighted ? 1 : 0, &cc, nullptr, nullptr, nullptr);
   if (s != DAWN_OK) die(s, "dawn_closeness");
   return cc;
+}
+
+float BC_GPU::Betweenness_Centrality(Graph::Graph_t& graph, std::string& output_path) {
+  Device dev(graph, false);
+  std::vector<int32_t> sources(graph.rows);
+  for (int i = 0; i < graph.rows; i++) sources[i] = i;
+  std::vector<double> bc(graph.rows);
+  dawn_stats st;
+  const dawn_status s = dawn_betweenness(dev.g, sources.data(), graph.rows, bc.data(), &st);
+  if (s != DAWN_OK) die(s, "dawn_betweenness");
+  std::vector<float> out(bc.begin(), bc.end());
+  IO::outfile(graph.rows, out.data(), output_path);
+  return st.device_ms / 1000.0f;
 }
 
 }  // namespace DAWN

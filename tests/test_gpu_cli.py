@@ -71,3 +71,19 @@ def test_isolated_source_exits_zero(goldens):
     iso = int(np.nonzero(np.diff(g.row_ptr) == 0)[0][0])
     log = run("bfs_gpu", "-i", g.mtx, "-s", str(iso))
     assert f"Source [{iso}] is isolated node" in log
+
+
+def test_bc_tool(goldens, tmp_path):
+    # bc_gpu with the CPU tool's interface: "vertex value" lines (%.6f) for
+    # the non-zero betweenness values of every vertex, all vertices sources
+    import oracle as O
+    for g in goldens:
+        out = str(tmp_path / (g.name + ".bc.txt"))
+        log = run("bc_gpu", "-i", g.mtx, "-o", out)
+        assert "Nodes:" in log and "Edges:" in log and "Time:" in log
+        got = np.zeros(g.n)
+        for line in open(out):
+            j, v = line.split()
+            got[int(j)] = float(v)
+        want = O.bc(g)
+        np.testing.assert_allclose(got, want, rtol=1e-4, atol=2e-6 + 1e-6 * float(np.abs(want).max()))
