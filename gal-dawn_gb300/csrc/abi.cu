@@ -793,6 +793,16 @@ dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value) 
       }
       g->auto_learned = value != 0;
       return DAWN_OK;
+    case DAWN_OPT_L2_PERSIST:
+      if (value != 0 && value != 1) {
+        dawn::set_error("L2 persist must be 0 or 1");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      if (g->l2_persist != (value != 0)) {
+        g->l2_persist = value != 0;
+        dawn::drop_graphs(g);  // the window is an attribute of the captured kernel nodes
+      }
+      return DAWN_OK;
     default:
       dawn::set_error("unknown option %d", option);
       return DAWN_ERR_INVALID_ARG;
@@ -879,6 +889,9 @@ dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option, int64_t* 
       return DAWN_OK;
     case DAWN_OPT_AUTO_LEARNED:
       *value = g->auto_learned ? 1 : 0;
+      return DAWN_OK;
+    case DAWN_OPT_L2_PERSIST:
+      *value = g->l2_persist ? 1 : 0;
       return DAWN_OK;
     default:
       dawn::set_error("unknown option %d", option);

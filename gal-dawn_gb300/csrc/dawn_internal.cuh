@@ -123,6 +123,10 @@ struct SsFamily {
   int* in_graph = nullptr;
   // device address of the int32 `done` flag polled by the host loop
   const void* done_flag = nullptr;
+  // L2 persisting window for the body kernels (hot arrays re-read at every
+  // level); l2_bytes = 0: none
+  const void* l2_base = nullptr;
+  size_t l2_bytes = 0;
   // traced form: the control block and how to read it
   const void* ctl = nullptr;
   size_t ctl_bytes = 0;
@@ -210,6 +214,7 @@ struct dawn_graph {
   int32_t pull_seg = 1024;      // heavy pull rows: in-edges per warp task (rows of >= 2x are cut)
   int32_t static_seg = 0;       // pull_seg the static pull lists were built with
   bool auto_learned = false;    // DAWN_VARIANT_AUTO batched calls use the learned selector
+  bool l2_persist = false;      // DAWN_OPT_L2_PERSIST: persisting L2 window on the frontier words
   // Learned selector.  The decide kernels take the slot's address as a
   // launch argument (fixed for the handle's life, so captured graphs stay
   // valid) and prefetch it while they read the control block.

@@ -1180,6 +1180,11 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   fam.ctl = a.ctl;
   fam.ctl_bytes = sizeof(BsCtl);
   fam.probe = probe_bs;
+  if (g->l2_persist) {
+    // the three rotating frontier slots: every pull level gathers from one
+    fam.l2_base = a.fr;
+    fam.l2_bytes = sizeof(u64) * 3 * W * nn;
+  }
   fam.handle = &a.handle;
   fam.in_graph = &a.in_graph;
   fam.done_flag = &a.ctl->done;

@@ -88,7 +88,45 @@ dawn_status download_ctl(dawn_graph* g, SsCtl* out) {
 
 namespace {
 
-dawn_status add_kernel(cudaGraph_t graph, cudaGraphNode_t* node, const cudaGraphNode_t* dep, const Launch& l) {
+// The persisting-L2 carve-out of each device, set once to the device's
+// maximum (a limit of this process's context; it ends with the process).
+struct L2Persist {
+  std::once_flag once;
+  size_t carve = 0, max_window = 0;
+};
+L2Persist g_l2[64];
+
+// Access-policy window of a family's body kernels: its hot arrays (the
+// frontier words every level gathers from) marked persisting, so the edge
+// arrays that stream through L2 at every level do not evict them.
+bool family_window(const SsFamily& fam, cudaAccessPolicyWindow* w) {
+  if (!fam.l2_base || fam.l2_bytes == 0) return false;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  L2Persist& p = g_l2[dev];
+  std::call_once(p.once, [&p, dev] {
+    int carve = 0, win = 0;
+    if (cudaDeviceGetAttribute(&carve, cudaDevAttrMaxPersistingL2CacheSize, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&win, cudaDevAttrMaxAccessPolicyWindowSize, dev) != cudaSuccess || carve <= 0 ||
+        win <= 0 || cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)carve) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    p.carve = (size_t)carve;
+    p.max_window = (size_t)win;
+  });
+  if (p.carve == 0) return false;
+  w->base_ptr = const_cast<void*>(fam.l2_base);
+  w->num_bytes = fam.l2_bytes < p.max_window ? fam.l2_bytes : p.max_window;
+  w->hitRatio = (float)((double)p.carve / (double)w->num_bytes);
+  if (w->hitRatio > 1.0f) w->hitRatio = 1.0f;
+  w->hitProp = cudaAccessPropertyPersisting;
+  w->missProp = cudaAccessPropertyStreaming;
+  return true;
+}
+
+dawn_status add_kernel(cudaGraph_t graph, cudaGraphNode_t* node, const cudaGraphNode_t* dep, const Launch& l,
+                       const cudaAccessPolicyWindow* w = nullptr) {
   cudaKernelNodeParams p = {};
   p.func = const_cast<void*>(l.fn);
   p.gridDim = l.grid;
@@ -97,6 +135,11 @@ dawn_status add_kernel(cudaGraph_t graph, cudaGraphNode_t* node, const cudaGraph
   p.kernelParams = l.args;
   p.extra = nullptr;
   DAWN_CUDA(cudaGraphAddKernelNode(node, graph, dep, dep ? 1 : 0, &p));
+  if (w) {
+    cudaKernelNodeAttrValue v = {};
+    v.accessPolicyWindow = *w;
+    DAWN_CUDA(cudaGraphKernelNodeSetAttribute(*node, cudaKernelNodeAttributeAccessPolicyWindow, &v));
+  }
   return DAWN_OK;
 }
 
@@ -132,9 +175,11 @@ dawn_status build_graph(SsFamily& fam, cudaGraphExec_t* exec) {
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     *fam.handle = h;
     *fam.in_graph = 1;
+    cudaAccessPolicyWindow win;
+    const bool has_win = family_window(fam, &win);
     cudaGraphNode_t bprev = nullptr;
     for (int i = 0; i < fam.nbody && st == DAWN_OK; i++) {
-      st = add_kernel(body, &node, bprev ? &bprev : nullptr, fam.body[i]);
+      st = add_kernel(body, &node, bprev ? &bprev : nullptr, fam.body[i], has_win ? &win : nullptr);
       bprev = node;
     }
     if (st != DAWN_OK) break;
@@ -158,8 +203,22 @@ dawn_status build_graph(SsFamily& fam, cudaGraphExec_t* exec) {
   return st;
 }
 
-dawn_status launch(const Launch& l, cudaStream_t s) {
-  DAWN_CUDA(cudaLaunchKernel(l.fn, l.grid, l.block, l.args, 0, s));
+dawn_status launch(const Launch& l, cudaStream_t s, const cudaAccessPolicyWindow* w = nullptr) {
+  if (!w) {
+    DAWN_CUDA(cudaLaunchKernel(l.fn, l.grid, l.block, l.args, 0, s));
+    return DAWN_OK;
+  }
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeAccessPolicyWindow;
+  attr.val.accessPolicyWindow = *w;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = l.grid;
+  cfg.blockDim = l.block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cfg.attrs = &attr;
+  cfg.numAttrs = 1;
+  DAWN_CUDA(cudaLaunchKernelExC(&cfg, l.fn, l.args));
   return DAWN_OK;
 }
 
@@ -171,6 +230,8 @@ constexpr int kPollLevels = 4;  // host-loop form: levels launched between polls
 // that does work at that level, one trace record per kernel.
 dawn_status ss_run_traced(dawn_graph* g, SsFamily& fam, int32_t nruns) {
   *fam.in_graph = 0;
+  cudaAccessPolicyWindow win;
+  const bool has_win = family_window(fam, &win);
   for (int i = 0; i < 10; i++)
     if (!g->trace_ev[i]) DAWN_CUDA(cudaEventCreate(&g->trace_ev[i]));
   std::vector<unsigned char> host(fam.ctl_bytes);
@@ -208,11 +269,11 @@ dawn_status ss_run_traced(dawn_graph* g, SsFamily& fam, int32_t nruns) {
       for (int b = 0; b + 1 < fam.nbody; b++) {
         if (fam.body[b].mode >= 0 && fam.body[b].mode != p.mode) continue;
         DAWN_CUDA(cudaEventRecord(g->trace_ev[2 * np], g->stream));
-        DAWN_CHECK(launch(fam.body[b], g->stream));
+        DAWN_CHECK(launch(fam.body[b], g->stream, has_win ? &win : nullptr));
         DAWN_CUDA(cudaEventRecord(g->trace_ev[2 * np + 1], g->stream));
         pend[np++] = {b, p};
       }
-      DAWN_CHECK(launch(fam.body[fam.nbody - 1], g->stream));
+      DAWN_CHECK(launch(fam.body[fam.nbody - 1], g->stream, has_win ? &win : nullptr));
       DAWN_CUDA(cudaStreamSynchronize(g->stream));
       for (int i = 0; i < np; i++) {
         dawn_trace_rec r = {};
@@ -248,12 +309,14 @@ dawn_status ss_run(dawn_graph* g, SsFamily& fam, int32_t nruns, cudaGraphExec_t*
     return DAWN_OK;
   }
   *fam.in_graph = 0;
+  cudaAccessPolicyWindow win;
+  const bool has_win = family_window(fam, &win);
   int32_t* h_done = &g->h_ctl[1].done;
   for (int32_t i = 0; i < nruns; i++) {
     for (int j = 0; j < fam.npre; j++) DAWN_CHECK(launch(fam.pre[j], g->stream));
     for (;;) {
       for (int j = 0; j < kPollLevels; j++)
-        for (int b = 0; b < fam.nbody; b++) DAWN_CHECK(launch(fam.body[b], g->stream));
+        for (int b = 0; b < fam.nbody; b++) DAWN_CHECK(launch(fam.body[b], g->stream, has_win ? &win : nullptr));
       DAWN_CUDA(cudaMemcpyAsync(h_done, fam.done_flag, sizeof(int32_t), cudaMemcpyDeviceToHost, g->stream));
       DAWN_CUDA(cudaStreamSynchronize(g->stream));
       if (*h_done) break;

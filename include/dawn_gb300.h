@@ -256,6 +256,16 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources,
 #define DAWN_OPT_PULL_SEGMENT 5
 #define DAWN_OPT_BLOCKS_PER_SM 6
 #define DAWN_OPT_AUTO_LEARNED 7
+/*   DAWN_OPT_L2_PERSIST    1: the batched traversal's frontier words are
+ *                          marked persisting in L2 (an access-policy window on
+ *                          its level kernels; the device's persisting carve-out
+ *                          is set for the rest of this process), so the edge
+ *                          arrays streaming through L2 do not evict them.
+ *                          0 (default): no window.  Measured slower on RMAT
+ *                          scale 22 (1.74 -> 2.25 ms per 64 sources: the
+ *                          carve-out shrinks the L2 the gathers also use), even
+ *                          at scales 21 and 24. */
+#define DAWN_OPT_L2_PERSIST 8
 
 /* Autotuner (no counterpart in the reference, whose launch shapes are fixed
  * in its tools, algorithm/gpu/mssp_gpu/mssp_gpu.cu:16-17).  Times the

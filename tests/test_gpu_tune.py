@@ -73,3 +73,15 @@ def test_autotune_single_source():
         assert t["bitset_width"] == 0 and t["blocks_per_sm"] in (0, 1, 2, 4)
         d, _ = dg.bfs(srcs, variant=abi.VARIANT_DO)
         assert np.array_equal(d, want)
+
+
+def test_l2_window_changes_nothing():
+    g = gen.rmat(14, 16, seed=57)
+    srcs = gen.sources(g, 64, seed=58)
+    want, _ = expected(g, srcs)
+    with abi.Graph(g) as dg:
+        assert dg.get_option(abi.OPT_L2_PERSIST) == 0
+        for persist in (1, 0, 1):
+            dg.set_option(abi.OPT_L2_PERSIST, persist)
+            d, _ = dg.bfs(srcs, variant=abi.VARIANT_LEARNED)
+            assert np.array_equal(d, want), persist
