@@ -17,7 +17,8 @@
 //     128-entry segment at a time); lane i owns sources i and i + 32.  The
 //     warp loads 32 of the row's targets and weights in one coalesced read,
 //     then for each edge every lane relaxes its two sources against the
-//     target's distance row and applies atomicMin only where it improves;
+//     target's distance row (fetched for four edges at a time) and issues a
+//     return-free atomicMin where it improves on the fetched value;
 //     the improved sources are OR-ed into the target's next mask, and the
 //     first setter queues the target;
 //   * a final pass transposes the block into the caller's source-major rows
@@ -189,13 +190,24 @@ __global__ void __launch_bounds__(kBlock, 5) mw_push(const int32_t* __restrict__
           impA[i] = impB[i] = false;
           if (v[i] < 0) continue;
           int32_t* dv = D + (size_t)v[i] * kBatch;
+          // Improvement is judged against the row fetched above and the
+          // minimum is a reduction without a return value: a target whose
+          // entry another warp lowered further in the meantime is only
+          // relaxed once more at the next level, which leaves the fixed
+          // point unchanged.
           if (actA) {
             const int32_t c = relax(dA, wv[i], fl);
-            if (c < curA[i]) impA[i] = c < atomicMin(dv + lane, c);
+            if (c < curA[i]) {
+              atomicMin(dv + lane, c);
+              impA[i] = true;
+            }
           }
           if (actB) {
             const int32_t c = relax(dB, wv[i], fl);
-            if (c < curB[i]) impB[i] = c < atomicMin(dv + lane + 32, c);
+            if (c < curB[i]) {
+              atomicMin(dv + lane + 32, c);
+              impB[i] = true;
+            }
           }
         }
 #pragma unroll
