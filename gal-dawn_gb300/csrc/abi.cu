@@ -803,6 +803,13 @@ dawn_status dawn_graph_set_option(dawn_graph* g, int32_t option, int64_t value) 
         dawn::drop_graphs(g);  // the window is an attribute of the captured kernel nodes
       }
       return DAWN_OK;
+    case DAWN_OPT_SMALL_LEVELS:
+      if (value != 0 && value != 1) {
+        dawn::set_error("small levels must be 0 or 1");
+        return DAWN_ERR_INVALID_ARG;
+      }
+      g->small_levels = value != 0;  // read from the control block at every call
+      return DAWN_OK;
     default:
       dawn::set_error("unknown option %d", option);
       return DAWN_ERR_INVALID_ARG;
@@ -892,6 +899,9 @@ dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option, int64_t* 
       return DAWN_OK;
     case DAWN_OPT_L2_PERSIST:
       *value = g->l2_persist ? 1 : 0;
+      return DAWN_OK;
+    case DAWN_OPT_SMALL_LEVELS:
+      *value = g->small_levels ? 1 : 0;
       return DAWN_OK;
     default:
       dawn::set_error("unknown option %d", option);

@@ -15,6 +15,8 @@
 // alpha/beta rule) on the device.  Both kernels emit the next frontier as a
 // queue and as a bitmap, so either direction can follow.  Distances are
 // written once, when a vertex is claimed.
+#include <cooperative_groups.h>
+#include <climits>
 #include <mutex>
 
 #include "dawn_device.cuh"
@@ -24,6 +26,17 @@ namespace dawn {
 namespace {
 
 constexpr long long kAlpha = 14, kBeta = 24;
+
+// Small-frontier levels (bfs_small): one cluster of kSmallCtas CTAs runs
+// push levels back to back while the frontier stays within kSmallFrontier
+// vertices, kSmallEdges out-edges and kSmallCap vertices per CTA, at most
+// kSmallMaxLevels levels per launch.
+constexpr int kSmallCtas = 8;
+constexpr int kSmallBlock = 1024;
+constexpr int kSmallCap = 1536;
+constexpr int kSmallFrontier = 8192;
+constexpr long long kSmallEdges = 32768;
+constexpr int kSmallMaxLevels = 512;
 
 __device__ __forceinline__ uint32_t* rot(uint32_t* fbm, int i, int nwords) {
   return fbm + (size_t)(i % 3) * nwords;
@@ -125,6 +138,274 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }
 
+// Expands one warp batch of frontier rows: lane i holds row (rs, deg) when
+// valid.  Rows of >= kWarpRow entries are swept by the whole warp, shorter
+// ones are concatenated through a warp scan and dealt 32 edges at a time
+// (the owning lane is found by a binary search over the lanes' exclusive
+// offsets, through shuffles).  op(k, valid) runs on all 32 lanes.
+template <class Op>
+__device__ __forceinline__ void expand_rows(bool valid, int rs, int deg, Op&& op) {
+  const int lane = lane_id();
+  if (!valid) deg = 0;
+  uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
+  while (big) {
+    const int leader = __ffs(big) - 1;
+    big &= big - 1;
+    const int s = __shfl_sync(kFull, rs, leader), d = __shfl_sync(kFull, deg, leader);
+    for (int k0 = 0; k0 < d; k0 += 32) op(s + k0 + lane, k0 + lane < d);
+  }
+  const int sdeg = deg < kWarpRow ? deg : 0;
+  const int incl = warp_incl_scan(sdeg);
+  const int excl = incl - sdeg;
+  const int total = __shfl_sync(kFull, incl, 31);
+  for (int e0 = 0; e0 < total; e0 += 32) {
+    const int e = e0 + lane;
+    int lo = 0;  // last lane whose offset is <= e
+#pragma unroll
+    for (int step = 16; step; step >>= 1) {
+      const int ex = __shfl_sync(kFull, excl, lo + step);
+      if (ex <= e) lo += step;
+    }
+    const int k = __shfl_sync(kFull, rs, lo) + (e - __shfl_sync(kFull, excl, lo));
+    op(k, e < total);
+  }
+}
+
+// Rows per warp batch in bfs_small: the level's rows spread over all the
+// cluster's warps (fewer than 32 per warp when the frontier is small), so
+// that each warp's chain of dependent loads is short.
+__device__ __forceinline__ int batch_rows(int rows) {
+  constexpr int kLanes = kSmallCtas * kSmallBlock;
+  if (rows >= kLanes) return 32;
+  const int bs = (rows + kLanes / 32 - 1) / (kLanes / 32);
+  return bs < 1 ? 1 : bs;
+}
+
+// One CTA's share of one level's frontier in bfs_small: discovered vertices
+// with their row start and degree.
+struct SmallSlice {
+  int32_t u[kSmallCap];
+  int32_t rs[kSmallCap];
+  int32_t deg[kSmallCap];
+};
+
+// Small frontiers: a single cluster of kSmallCtas CTAs runs push levels one
+// after another in one launch.
+//   * Each CTA appends the vertices its warps discover to its own shared-
+//     memory slice (by level parity); the next level deals the rows of all
+//     the cluster's slices to the cluster's warps, reading them through
+//     distributed shared memory, so the frontier never goes through HBM.
+//   * One cluster barrier per level (release/acquire at cluster scope)
+//     orders the slices and the visited-bitmap claims; a kept vertex's
+//     distance is written when the next level reads it from its slice;
+//     after it every warp reads the eight slices' counters and takes the same
+//     continue/stop decision.  A CTA resets its slice of the other parity
+//     after the barrier: every reader of that slice (the level before) has
+//     arrived at it.
+//   * The loop stops after a level whose frontier is empty, holds a row of
+//     >= kLongRow entries, outgrows kSmallFrontier vertices, kSmallEdges
+//     out-edges or one slice (the entries past it went to the global queue
+//     at once), at level n - 1, or after kSmallMaxLevels levels.  That last
+//     level is handed to the per-level kernels in their format: slices ->
+//     global queue and segment lists, a fresh frontier bitmap of the level
+//     (the three rotating bitmaps are cleared first, since these levels did
+//     not maintain them), and the counters the decide kernel reads, which
+//     then does that level's bookkeeping as after a push.
+// The first level reads the global queue and segments the kernels before
+// wrote; its input counters are zeroed (behind one extra barrier) before a
+// later level of that parity can spill into them.
+__global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock)
+    bfs_small(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col, SsCtl* ctl, int32_t* q,
+              Seg* segs, size_t segcap, uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm, int32_t n,
+              int32_t nwords) {
+  __shared__ SmallSlice s_sl[2];
+  // per parity: vertices appended (past kSmallCap they spilled), whether
+  // one has a row of >= kLongRow entries, and their out-degree sum (the
+  // degrees of distinct vertices sum to at most m < 2^31)
+  __shared__ int32_t s_cnt[2], s_nlong[2];
+  __shared__ uint32_t s_mf[2];
+  if (ctl->done || ctl->mode != kModeSmall) return;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int lane = lane_id(), wib = threadIdx.x >> 5;
+  constexpr int kWarps = kSmallBlock / 32;
+  const int cwarp = rank * kWarps + wib;  // warp index within the cluster
+  int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
+  if (threadIdx.x < 2) {
+    s_cnt[threadIdx.x] = 0;
+    s_nlong[threadIdx.x] = 0;
+    s_mf[threadIdx.x] = 0;
+  }
+  __syncthreads();
+
+  int L = ctl->level;
+  int pre = INT_MAX, tot = 0;       // dealing of the previous level's slices (lane r < kSmallCtas: slice r)
+  unsigned long long sum_mf = 0;    // out-edges of the levels finished here
+  int nlev = 0, last_nf = 0, nf = 0;
+  unsigned long long mf = 0;
+  for (int iter = 0;; iter++) {
+    const int p = L & 1;
+    uint32_t my_mf = 0;
+    bool my_long = false;
+    auto op = [&](int k, bool valid) {
+      const int32_t u = valid ? __ldg(col + k) : -1;
+      bool found = false;
+      int rs = 0, deg = 0;
+      if (valid) {
+        // the row bounds are loaded alongside the claim (most claims
+        // succeed on small frontiers), so they add no round trip
+        const uint32_t bit = 1u << (u & 31);
+        rs = __ldg(row_ptr + u);
+        const int re = __ldg(row_ptr + u + 1);
+        found = !(atomicOr(vbm + (u >> 5), bit) & bit);
+        deg = re - rs;
+      }
+      if (found) {
+        my_mf += (uint32_t)deg;
+        my_long |= deg >= kLongRow;
+      }
+      const uint32_t m = __ballot_sync(kFull, found);
+      if (m == 0) return;
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&s_cnt[p], __popc(m));
+      const int slot = __shfl_sync(kFull, base, leader) + __popc(m & lanemask_lt());
+      if (found && slot < kSmallCap) {
+        s_sl[p].u[slot] = u;
+        s_sl[p].rs[slot] = rs;
+        s_sl[p].deg[slot] = deg;
+      }
+      const bool spill = found && slot >= kSmallCap;
+      if (spill) dist[u] = L;  // kept vertices get theirs when the next level reads them
+      if (__any_sync(kFull, spill))
+        emit_routed(spill, u, deg, rs, q + (size_t)p * n, &ctl->qsize[p], segs + (size_t)p * segcap, &ctl->lpack[p]);
+    };
+    if (iter == 0) {
+      // the previous level in the global format
+      const int pin = p ^ 1;
+      const int32_t* qin = q + (size_t)pin * n;
+      const int qn = ctl->qsize[pin], ln = seg_count(ctl->lpack[pin]);
+      seg_expand(row_ptr, segs + (size_t)pin * segcap, ln, [&](int32_t, int k, bool valid) { op(k, valid); });
+      const int bs = batch_rows(qn);
+      for (int b = cwarp * bs; b < qn; b += kSmallCtas * kWarps * bs) {
+        const int i = b + lane;
+        const bool ok = lane < bs && i < qn;
+        int rs = 0, deg = 0;
+        if (ok) {
+          const int32_t v = qin[i];
+          rs = row_ptr[v];
+          deg = row_ptr[v + 1] - rs;
+        }
+        expand_rows(ok, rs, deg, op);
+      }
+    } else {
+      // the previous level's slices, across the cluster
+      const int bs = batch_rows(tot);
+      for (int b = cwarp * bs; b < tot; b += kSmallCtas * kWarps * bs) {
+        const int e = lane < bs ? b + lane : INT_MAX;
+        int r = 0;  // last slice whose first index is <= e
+#pragma unroll
+        for (int step = kSmallCtas / 2; step; step >>= 1) {
+          const int ex = __shfl_sync(kFull, pre, r + step);
+          if (ex <= e) r += step;
+        }
+        const int off = e - __shfl_sync(kFull, pre, r);
+        int rs = 0, deg = 0;
+        if (e < tot) {
+          const SmallSlice* src = cluster.map_shared_rank(&s_sl[p ^ 1], r);
+          rs = src->rs[off];
+          deg = src->deg[off];
+          dist[src->u[off]] = L - 1;
+        }
+        expand_rows(e < tot, rs, deg, op);
+      }
+    }
+    my_mf = __reduce_add_sync(kFull, my_mf);
+    my_long = __any_sync(kFull, my_long);
+    if (lane == 0) {
+      if (my_mf) atomicAdd(&s_mf[p], my_mf);
+      if (my_long) s_nlong[p] = 1;
+    }
+    cluster.sync();
+    // this level's counters, slice by slice (lane r reads slice r)
+    int cnt = 0, nl = 0;
+    uint32_t mr = 0;
+    if (lane < kSmallCtas) {
+      cnt = *cluster.map_shared_rank(&s_cnt[p], lane);
+      nl = *cluster.map_shared_rank(&s_nlong[p], lane);
+      mr = *cluster.map_shared_rank(&s_mf[p], lane);
+    }
+    const int kept = cnt < kSmallCap ? cnt : kSmallCap;
+    int incl = kept;  // inclusive scan over the kSmallCtas slice lanes
+#pragma unroll
+    for (int d = 1; d < kSmallCtas; d <<= 1) {
+      const int t = __shfl_up_sync(kFull, incl, d);
+      if (lane >= d) incl += t;
+    }
+    nf = (int)__reduce_add_sync(kFull, (uint32_t)cnt);
+    mf = __reduce_add_sync(kFull, mr);
+    const bool longs = __any_sync(kFull, nl != 0);
+    const bool over = __any_sync(kFull, cnt > kSmallCap);
+    const bool stop = nf == 0 || longs || over || nf > kSmallFrontier || (long long)mf > kSmallEdges ||
+                      L + 1 >= n || iter + 1 == kSmallMaxLevels;
+    if (stop) break;
+    pre = lane < kSmallCtas ? incl - kept : INT_MAX;
+    tot = __shfl_sync(kFull, incl, kSmallCtas - 1);
+    sum_mf += mf;
+    nlev++;
+    last_nf = nf;
+    if (threadIdx.x == 0) {
+      s_cnt[p ^ 1] = 0;
+      s_nlong[p ^ 1] = 0;
+      s_mf[p ^ 1] = 0;
+      if (iter == 0 && rank == 0) {
+        ctl->qsize[p ^ 1] = 0;
+        ctl->lpack[p ^ 1] = 0;
+        ctl->mf[p ^ 1] = 0;
+      }
+    }
+    if (iter == 0) cluster.sync(); else __syncthreads();
+    L++;
+  }
+
+  // hand-off of level L (slice parity p) to the per-level kernels
+  const int p = L & 1;
+  const int mine = s_cnt[p] < kSmallCap ? s_cnt[p] : kSmallCap;
+  for (int b = wib * 32; b < mine; b += kWarps * 32) {
+    const int i = b + lane;
+    const bool ok = i < mine;
+    const int32_t u = ok ? s_sl[p].u[i] : 0;
+    if (ok) dist[u] = L;
+    emit_routed(ok, u, ok ? s_sl[p].deg[i] : 0, ok ? s_sl[p].rs[i] : 0, q + (size_t)p * n, &ctl->qsize[p],
+                segs + (size_t)p * segcap, &ctl->lpack[p]);
+  }
+  const size_t tid = (size_t)rank * kSmallBlock + threadIdx.x;
+  const size_t stride = (size_t)kSmallCtas * kSmallBlock;
+  for (size_t i = tid; i < (size_t)3 * nwords; i += stride) fbm[i] = 0;
+  if (rank == 0 && threadIdx.x == 0) {
+    ctl->mf[p] = mf;
+    ctl->reached += sum_mf;
+    ctl->mu -= (long long)sum_mf;
+    ctl->n_push += nlev;
+    if (nlev) ctl->prev_nf = last_nf;
+    ctl->level = L;
+  }
+  cluster.sync();
+  uint32_t* fcur = rot(fbm, L, nwords);
+  const int qn = __ldcg(&ctl->qsize[p]), ln = seg_count(__ldcg(&ctl->lpack[p]));
+  for (size_t i = tid; i < (size_t)qn; i += stride) {
+    const int32_t v = __ldcg(q + (size_t)p * n + i);
+    atomicOr(fcur + (v >> 5), 1u << (v & 31));
+  }
+  // a long row's segments are contiguous: its first one sets the bit
+  const Seg* sl = segs + (size_t)p * segcap;
+  for (size_t i = tid; i < (size_t)ln; i += stride) {
+    const int32_t v = __ldcg(&sl[i].v);
+    if (i == 0 || __ldcg(&sl[i - 1].v) != v) atomicOr(fcur + (v >> 5), 1u << (v & 31));
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ row_ptr,
                                                    const int32_t* __restrict__ t_row_ptr,
                                                    const int32_t* __restrict__ t_col, SsCtl* __restrict__ ctl,
@@ -212,7 +493,7 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, const float* __re
   if (lane == 0) {
     ctl->reached += mf;
     ctl->mu = mu;
-    if (cur_mode == kModePush) ctl->n_push++; else ctl->n_pull++;
+    if (cur_mode == kModePull) ctl->n_pull++; else ctl->n_push++;
   }
   if (nf == 0 || L >= n) {
     if (lane == 0) {
@@ -221,7 +502,7 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, const float* __re
     }
     return;
   }
-  int mode = cur_mode;
+  int mode = cur_mode == kModePull ? kModePull : kModePush;  // cluster levels are push levels
   if (policy == DAWN_VARIANT_DO) {
     if (mode == kModePush) {
       if ((long long)mf * kAlpha > mu && nf > prev_nf) mode = kModePull;
@@ -238,6 +519,11 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, const float* __re
     mode = sel_pick(sel_w, x, (1u << kVarPush) | (1u << kVarPull), h, ctl->sel_margin) == kVarPull ? kModePull
                                                                                                 : kModePush;
   }
+  // small levels start from frontiers without long rows: a long row's
+  // neighbourhood tends to hold more, which end the cluster levels at once
+  if (mode == kModePush && ctl->small && !force && policy == DAWN_VARIANT_DO && nf <= kSmallFrontier &&
+      (long long)mf <= kSmallEdges && long_vertices(ctl->lpack[pout]) == 0)
+    mode = kModeSmall;
   if (lane == 0) {
     ctl->qsize[pout ^ 1] = 0;
     ctl->lpack[pout ^ 1] = 0;
@@ -291,6 +577,7 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   c.use_sel = g->sel_call;
   c.sel_margin = g->sel_margin;
   c.force = g->force_variant == 3 ? 1 + kVarPush : g->force_variant;
+  c.small = g->small_levels ? 1 : 0;
   c.m = m;
   DAWN_CHECK(upload_ctl(g, c));
 
@@ -329,6 +616,7 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   void* push_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm, &a.n, &a.nwords};
   void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm,
                        &a.n, &a.nwords};
+  void* small_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm, &a.n, &a.nwords};
   void* decide_args[] = {&a.ctl, &a.n, &a.sel_w, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
 
@@ -337,12 +625,13 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   fam.npre = 2;
   fam.pre[0] = {(const void*)bfs_clear, clear_args, dim3(sms * 4), dim3(kBlock)};
   fam.pre[1] = {(const void*)bfs_init, init_args, dim3(1), dim3(32)};
-  fam.nbody = 3;
+  fam.nbody = 4;
   fam.body[0] = {(const void*)bfs_push, push_args, dim3(persistent_blocks((const void*)bfs_push, kBlock, 0, g->blocks_per_sm)),
                  dim3(kBlock), "bfs_push", kModePush};
   fam.body[1] = {(const void*)bfs_pull, pull_args, dim3(persistent_blocks((const void*)bfs_pull, kBlock, 0, g->blocks_per_sm)),
                  dim3(kBlock), "bfs_pull", kModePull};
-  fam.body[2] = {(const void*)bfs_decide, decide_args, dim3(1), dim3(32), "bfs_decide"};
+  fam.body[2] = {(const void*)bfs_small, small_args, dim3(kSmallCtas), dim3(kSmallBlock), "bfs_small", kModeSmall};
+  fam.body[3] = {(const void*)bfs_decide, decide_args, dim3(1), dim3(32), "bfs_decide"};
   fam.npost = 1;
   fam.post[0] = {(const void*)ss_next, next_args, dim3(1), dim3(32), "ss_next"};
   fam.ctl = a.ctl;

@@ -80,8 +80,9 @@ constexpr int kWarpRow = 32;  // rows with at least this many entries use the wh
 // dealt 32 edges at a time.  op(v, k, valid) runs on all 32 lanes in
 // lockstep (it may use warp collectives); when valid, k is a CSR position in
 // the row of vertex v.  s_excl / s_rs / s_v are this warp's 32-entry
-// shared-memory scratch.
-template <class Op>
+// shared-memory scratch.  kCoherent reads the queue through L2 (a queue
+// written earlier in the same launch must not come from the read-only path).
+template <bool kCoherent = false, class Op>
 __device__ __forceinline__ void warp_expand(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ qin,
                                             int qn, int* s_excl, int* s_rs, int* s_v, Op&& op) {
   const int lane = lane_id();
@@ -90,7 +91,7 @@ __device__ __forceinline__ void warp_expand(const int32_t* __restrict__ row_ptr,
     int32_t v = -1;
     int rs = 0, re = 0;
     if (idx < qn) {
-      v = qin[idx];
+      v = kCoherent ? __ldcg(qin + idx) : qin[idx];
       rs = row_ptr[v];
       re = row_ptr[v + 1];
     }
@@ -153,6 +154,23 @@ __host__ __device__ inline size_t seg_capacity(int32_t n, long long m) {
   return 2 * (size_t)(m / kSeg) + 64;
 }
 
+// The whole warp writes the segments of every lane in lm (nseg segments
+// of lane l's row from CSR position rs, at list index first): a hub's
+// thousands of segments go out 32 per store instead of one lane writing
+// them all.
+__device__ __forceinline__ void write_segments(uint32_t lm, int32_t u, int rs, int nseg, uint32_t first,
+                                               Seg* __restrict__ segs) {
+  const int lane = lane_id();
+  while (lm) {
+    const int l = __ffs(lm) - 1;
+    lm &= lm - 1;
+    const int32_t lu = __shfl_sync(kFull, u, l);
+    const int lrs = __shfl_sync(kFull, rs, l), ln = __shfl_sync(kFull, nseg, l);
+    const uint32_t lf = __shfl_sync(kFull, first, l);
+    for (int j = lane; j < ln; j += 32) segs[lf + j] = Seg{lu, lrs + j * kSeg};
+  }
+}
+
 // Queues a discovered vertex: short rows as a vertex, long rows as segments.
 // lpack packs (long vertices << 32 | segments) so one atomicAdd per warp
 // reserves the warp's segment slots.  All 32 lanes must call it.
@@ -171,7 +189,7 @@ __device__ __forceinline__ void emit_routed(bool found, int32_t u, int deg, int 
     unsigned long long base = 0;
     if (lane_id() == 0) base = atomicAdd(lpack, ((unsigned long long)__popc(lm) << 32) | (unsigned)tot);
     const uint32_t b = (uint32_t)__shfl_sync(kFull, base, 0);
-    for (int j = 0; j < nseg; j++) segs[b + incl - nseg + j] = Seg{u, rs + j * kSeg};
+    write_segments(lm, u, rs, nseg, b + incl - nseg, segs);
   }
 }
 
@@ -179,13 +197,19 @@ __device__ __forceinline__ int seg_count(unsigned long long lpack) { return (int
 __device__ __forceinline__ int long_vertices(unsigned long long lpack) { return (int)(lpack >> 32); }
 
 // Deals segments to warps (one segment per warp at a time, one lane per
-// edge).  op(v, k, valid) as in warp_expand.
-template <class Op>
+// edge).  op(v, k, valid) as in warp_expand; kCoherent as there.
+template <bool kCoherent = false, class Op>
 __device__ __forceinline__ void seg_expand(const int32_t* __restrict__ row_ptr, const Seg* __restrict__ segs,
                                            int nsegs, Op&& op) {
   const int lane = lane_id();
   for (int i = global_warp(); i < nsegs; i += num_warps()) {
-    const Seg sg = segs[i];
+    Seg sg;
+    if (kCoherent) {
+      sg.v = __ldcg(&segs[i].v);
+      sg.k0 = __ldcg(&segs[i].k0);
+    } else {
+      sg = segs[i];
+    }
     const int e = min(sg.k0 + kSeg, row_ptr[sg.v + 1]);
     for (int k0 = sg.k0; k0 < e; k0 += 32) op(sg.v, k0 + lane, k0 + lane < e);
   }
@@ -245,7 +269,7 @@ __device__ __forceinline__ void emit_routed(bool found, int32_t u, int deg, int 
     unsigned long long base = 0;
     if (lane_id() == 0) base = atomicAdd(lpack, ((unsigned long long)__popc(lm) << 32) | (unsigned)tot);
     const uint32_t b = (uint32_t)__shfl_sync(kFull, base, 0);
-    for (int j = 0; j < nseg; j++) segs[b + incl - nseg + j] = Seg{u, rs + j * kSeg};
+    write_segments(lm, u, rs, nseg, b + incl - nseg, segs);
   }
 }
 

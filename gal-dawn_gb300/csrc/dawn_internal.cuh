@@ -54,7 +54,8 @@ void pool_free(void* p, cudaStream_t s);
 
 // --- single-source frontier traversal (BOVM push/pull, GOVM push) ---------
 
-enum : int32_t { kModePush = 0, kModePull = 1 };
+// kModeSmall: small frontiers, several push levels in one cluster launch
+enum : int32_t { kModePush = 0, kModePull = 1, kModeSmall = 2 };
 
 // Device-resident control block of one single-source traversal.  Every
 // per-level kernel reads its parameters from here, so the same launches
@@ -84,7 +85,7 @@ struct SsCtl {
   float sel_margin;             // log2 margin by which the selector must beat the heuristic
   int32_t work;                 // weighted pull: dynamic work counter (light rows)
   int32_t hwork;                // weighted pull: dynamic work counter (heavy-row segments)
-  int32_t pad4;
+  int32_t small;                // single-source BFS: 1 = small frontiers may run as cluster levels
   long long m;                  // CSR entries (selector input)
   // accumulated over all sources of the call
   unsigned long long total_reached;
@@ -215,6 +216,7 @@ struct dawn_graph {
   int32_t static_seg = 0;       // pull_seg the static pull lists were built with
   bool auto_learned = false;    // DAWN_VARIANT_AUTO batched calls use the learned selector
   bool l2_persist = false;      // DAWN_OPT_L2_PERSIST: persisting L2 window on the frontier words
+  bool small_levels = true;     // DAWN_OPT_SMALL_LEVELS: small frontiers as cluster levels
   // Learned selector.  The decide kernels take the slot's address as a
   // launch argument (fixed for the handle's life, so captured graphs stay
   // valid) and prefetch it while they read the control block.

@@ -29,6 +29,7 @@ EXPORTS = ("dawn_graph_create", "dawn_graph_create_device", "dawn_graph_destroy"
            "dawn_multi_closeness", "dawn_trace_enable", "dawn_trace_read", "dawn_last_error", "dawn_version")
 OPT_BITSET_WIDTH, OPT_PUSH_RATIO, OPT_FORCE_VARIANT, OPT_SELECTOR_MARGIN = 1, 2, 3, 4
 OPT_PULL_SEGMENT, OPT_BLOCKS_PER_SM, OPT_AUTO_LEARNED, OPT_L2_PERSIST = 5, 6, 7, 8
+OPT_SMALL_LEVELS = 9
 TUNE_USE_CACHE = 1
 SELECTOR_WEIGHTS = 1475
 

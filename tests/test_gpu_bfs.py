@@ -209,3 +209,48 @@ def test_random_selector_changes_nothing(seed):
         dg.set_selector(None)
         d, _ = dg.bfs(srcs, variant=abi.VARIANT_BITSET)
         assert np.array_equal(d, want)
+
+
+def directed_path(n):
+    rp = np.arange(n + 1, dtype=np.int32)
+    rp[-1] = n - 1
+    return gen.CsrGraph(n, rp, np.arange(1, n, dtype=np.int32))
+
+
+def test_small_levels_change_nothing():
+    # single-source direction-optimising BFS with stretches of small levels
+    # run inside one cluster launch, against the same calls with every level
+    # its own launch: distances (against the oracle), edge counts and level
+    # counts agree.  The path has more levels than one cluster launch runs;
+    # RMAT frontiers grow past the small limits and shrink back; the hub
+    # graph sends long rows through the segment lists inside the cluster.
+    hub = gen.rmat(12, 4, seed=51)
+    rp = np.concatenate([[0], np.cumsum(np.diff(hub.row_ptr) + np.where(np.arange(hub.n) == 7, 3000, 0))])
+    col = []
+    for v in range(hub.n):
+        col.append(hub.col[hub.row_ptr[v]:hub.row_ptr[v + 1]])
+        if v == 7:
+            col.append(np.random.default_rng(52).integers(0, hub.n, 3000))
+    hub = gen.CsrGraph(hub.n, rp.astype(np.int32), np.concatenate(col).astype(np.int32))
+    cases = [(directed_path(1500), np.array([0, 700, 1499], np.int32)),
+             (gen.grid(60, 170), np.array([0, 60 * 170 - 1, 5000], np.int32)),
+             (gen.rmat(14, 8, seed=53), None),
+             (hub, np.array([7, 8, 9], np.int32))]
+    for g, srcs in cases:
+        if srcs is None:
+            srcs = gen.sources(g, 4, seed=54)
+        want, edges = expected(g, srcs)
+        with abi.Graph(g) as dg:
+            assert dg.get_option(abi.OPT_SMALL_LEVELS) == 1
+            on, st_on = dg.bfs(srcs, variant=abi.VARIANT_DO)
+            dg.trace(True)
+            traced, _ = dg.bfs(srcs, variant=abi.VARIANT_DO)
+            dg.trace(False)
+            dg.set_option(abi.OPT_SMALL_LEVELS, 0)
+            off, st_off = dg.bfs(srcs, variant=abi.VARIANT_DO)
+        for d in (on, traced, off):
+            bad = np.argwhere(d != want)
+            assert bad.size == 0, (g.n, bad[:5])
+        assert st_on.edges_traversed == st_off.edges_traversed == edges
+        assert st_on.levels == st_off.levels
+        assert st_on.push_levels + st_on.pull_levels == st_off.push_levels + st_off.pull_levels
