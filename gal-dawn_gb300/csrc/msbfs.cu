@@ -21,11 +21,17 @@
 //         atomicOr-ed into `next`, and an update pass folds `next` into
 //         visited / frontier (over the touched list, or densely for large
 //         frontiers).
-// Neither writes distances during the traversal: the level at which a bit
+// Below level kDeepLevel neither writes distances: the level at which a bit
 // first appears is recorded in bit-sliced level words (slice k holds bit k
 // of the level of every (source, vertex) pair), and a final pass expands
 // them into the distance block with full-line coalesced stores, writing -1
-// for pairs never reached.
+// for pairs never reached.  From kDeepLevel on (high-diameter graphs, whose
+// vertices gain their bits one source at a time over thousands of levels) a
+// new bit is written out directly instead: one store per (source, vertex)
+// pair rather than a read-modify-write of every set bit's slice, and the
+// final pass leaves those entries alone.
+#include <algorithm>
+
 #include "dawn_device.cuh"
 #include "selector.cuh"
 
@@ -71,6 +77,9 @@ struct BsCtl {
 };
 
 constexpr int kSlicesCleared = 4;  // slices zeroed per batch; higher ones on first use
+constexpr int kDeepLevel = 32;     // levels from here on are written out directly
+constexpr int kShallowBits = 5;    // level slices kept: the bits of levels below kDeepLevel
+static_assert(kDeepLevel == 1 << kShallowBits, "slices hold exactly the levels below kDeepLevel");
 // Heavy pull rows: a row of at least 2 x seg in-edges (seg = the handle's
 // pull segment, 1024 by default) is cut into seg-entry warp tasks.
 
@@ -83,6 +92,20 @@ __device__ __forceinline__ u64 warp_or64(u64 x) {
   const unsigned lo = __reduce_or_sync(kFull, (unsigned)x);
   const unsigned hi = __reduce_or_sync(kFull, (unsigned)(x >> 32));
   return ((u64)hi << 32) | lo;
+}
+
+// 32 x 32 bit transpose across a warp: lane i holds row i on entry and
+// column i on exit (bit j of lane i's result = bit i of lane j's input).
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+  const int lane = lane_id();
+  const uint32_t left[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+  for (int t = 0; t < 5; t++) {
+    const int s = 16 >> t;
+    const uint32_t y = __shfl_xor_sync(kFull, x, s);
+    x = (lane & s) ? ((x & ~left[t]) | ((y & ~left[t]) >> s)) : ((x & left[t]) | ((y & left[t]) << s));
+  }
+  return x;
 }
 
 // W words of one vertex.
@@ -196,14 +219,49 @@ struct Bits {
   }
 };
 
-// Records the level of newly reached (source, vertex) pairs: slice k of
-// vertex u gains nw for every set bit k of the level.  The caller owns u.
+// Records the level of newly reached (source, vertex) pairs.  Below
+// kDeepLevel slice k of vertex u gains nw for every set bit k of the level.
+// From kDeepLevel on the level is stored at once: in the batch's distance
+// rows, or in u's level row (level mode); closeness mode sums it per source
+// instead (add_deep_sums).  The caller owns u.
 template <int W>
-__device__ __forceinline__ void record_level(u64* __restrict__ slices, int32_t n, int32_t u, const Bits<W>& nw,
-                                             int32_t level) {
-  for (unsigned L = (unsigned)level; L; L &= L - 1) {
-    u64* p = slices + ((size_t)(__ffs(L) - 1) * n + u) * W;
-    (Bits<W>::ld(p) | nw).st(p);
+__device__ __forceinline__ void record_level(const BsCtl* __restrict__ ctl, u64* __restrict__ slices, int32_t n,
+                                             int32_t u, const Bits<W>& nw, int32_t level) {
+  if (level < kDeepLevel) {
+    for (unsigned L = (unsigned)level; L; L &= L - 1) {
+      u64* p = slices + ((size_t)(__ffs(L) - 1) * n + u) * W;
+      (Bits<W>::ld(p) | nw).st(p);
+    }
+    return;
+  }
+  if (ctl->cc_sum) return;
+  if (ctl->lv_block) {
+    int32_t* row = ctl->lv_block + (size_t)u * 64;
+    for (u64 b = nw.w[0]; b; b &= b - 1) row[__ffsll((long long)b) - 1] = level;
+    return;
+  }
+  int32_t* dist = ctl->dist_base + (size_t)ctl->batch * 64 * W * n;
+#pragma unroll
+  for (int i = 0; i < W; i++)
+    for (u64 b = nw.w[i]; b; b &= b - 1) dist[(size_t)(64 * i + __ffsll((long long)b) - 1) * n + u] = level;
+}
+
+// Closeness mode from kDeepLevel on: adds the levels of the warp's new bits
+// to the batch's per-source sums.  The warp's 32 new-bit words are
+// transposed so lane j counts the bits of sources 64i + j and 64i + 32 + j
+// with popc; one atomic per lane and nonzero sum.  All 32 lanes call it (nw
+// zero where a lane has no vertex).
+template <int W>
+__device__ __forceinline__ void add_deep_sums(const BsCtl* __restrict__ ctl, const Bits<W>& nw, int32_t level) {
+  const size_t row0 = (size_t)ctl->batch * 64 * W;
+  const int lane = lane_id();
+#pragma unroll
+  for (int i = 0; i < W; i++) {
+    if (!__any_sync(kFull, nw.w[i] != 0ull)) continue;
+    const unsigned lo = __popc(warp_transpose32((uint32_t)nw.w[i]));
+    const unsigned hi = __popc(warp_transpose32((uint32_t)(nw.w[i] >> 32)));
+    if (lo) atomicAdd(ctl->cc_sum + row0 + 64 * i + lane, (unsigned long long)lo * (unsigned)level);
+    if (hi) atomicAdd(ctl->cc_sum + row0 + 64 * i + 32 + lane, (unsigned long long)hi * (unsigned)level);
   }
 }
 
@@ -387,6 +445,7 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
   LevelAcc acc;
   WarpQueue qa(s_qa[wib], aq_out, aq_count);
   WarpQueue qu(s_qu[wib], ul_out, ul_count);
+  const bool deep_cc = ctl->cc_sum && L >= kDeepLevel;
 
   for (;;) {
     int sidx = 0;
@@ -445,12 +504,13 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
       if (nw.any()) {
         (vis | nw).st(visit + (size_t)u * W);
         nw.st(fout + (size_t)u * W);
-        record_level<W>(slices, n, u, nw, L);
+        record_level<W>(ctl, slices, n, u, nw, L);
         ors = row_ptr[u];
         odeg = row_ptr[u + 1] - ors;
         acc.add((u64)odeg, (u64)(rend - rbeg), nw.popc(), (vis | nw) == full);
       }
     }
+    if (deep_cc) add_deep_sums<W>(ctl, nw, L);
     emit_routed(nw.any(), u, odeg, ors, qa, seg_out, al_pack);
   }
 
@@ -538,11 +598,12 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
     if (has) {
       (vis | nw).st(visit + (size_t)u * W);
       nw.st(fout + (size_t)u * W);
-      record_level<W>(slices, n, u, nw, L);
+      record_level<W>(ctl, slices, n, u, nw, L);
       ors = row_ptr[u];
       odeg = row_ptr[u + 1] - ors;
       acc.add((u64)odeg, (u64)deg, nw.popc(), !still);
     }
+    if (deep_cc) add_deep_sums<W>(ctl, nw, L);
     qu.push(still, u);
     emit_routed(has, u, odeg, ors, qa, seg_out, al_pack);
   }
@@ -628,6 +689,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
   const int tn = dense ? n : ctl->tq_size;
   WarpQueue wq(s_q[threadIdx.x >> 5], aq_out, &ctl->aq_size[L % 3]);
   LevelAcc acc;
+  const bool deep_cc = ctl->cc_sum && L >= kDeepLevel;
   const int total = gridDim.x * blockDim.x;
   for (int base = blockIdx.x * blockDim.x; base < tn; base += total) {
     const int i = base + threadIdx.x;
@@ -645,13 +707,14 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
         if (nw.any()) {
           (vis | nw).st(visit + (size_t)u * W);
           nw.st(fout + (size_t)u * W);
-          record_level<W>(slices, n, u, nw, L);
+          record_level<W>(ctl, slices, n, u, nw, L);
           ors = row_ptr[u];
           odeg = row_ptr[u + 1] - ors;
           acc.add((u64)odeg, (u64)(t_row_ptr[u + 1] - t_row_ptr[u]), nw.popc(), (vis | nw) == full);
         }
       }
     }
+    if (deep_cc) add_deep_sums<W>(ctl, nw, L);
     emit_routed(nw.any(), u, odeg, ors, wq, seg_out, &ctl->alpack[L % 3]);
   }
   wq.flush();
@@ -660,26 +723,33 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
 
 // Expands the level slices of one batch into its distance rows: thread per
 // vertex, one store per source, consecutive vertices per warp (full lines).
-// NB is the number of level bits in use (template for the common <= 8).
+// NB is the number of level bits in use (<= kShallowBits).  src is the
+// batch's source list when the traversal went past kDeepLevel, else NULL:
+// then a reached pair whose slice bits are all zero is either the source
+// itself (level 0) or was written out during the traversal, and is kept.
 template <int W, int NB>
 __device__ __forceinline__ void emit_vertex(int32_t* __restrict__ dist, int32_t n, int nb_src, size_t u,
                                             const u64* __restrict__ visit, const u64* __restrict__ slices,
-                                            int nbits) {
+                                            const int32_t* __restrict__ src) {
 #pragma unroll
   for (int i = 0; i < W; i++) {
     if (64 * i >= nb_src) break;
     const u64 vis = visit[u * W + i];
-    u64 w[NB > 0 ? NB : 1];
+    u64 w[NB];
+    u64 any = 0ull;
 #pragma unroll
-    for (int k = 0; k < NB; k++) w[k] = slices[((size_t)k * n + u) * W + i];
+    for (int k = 0; k < NB; k++) {
+      w[k] = slices[((size_t)k * n + u) * W + i];
+      any |= w[k];
+    }
     const int cnt = min(64, nb_src - 64 * i);
     for (int s = 0; s < cnt; s++) {
       int32_t v = -1;
       if ((vis >> s) & 1ull) {
+        if (src && !((any >> s) & 1ull) && src[64 * i + s] != (int32_t)u) continue;  // written at its level
         v = 0;
 #pragma unroll
         for (int k = 0; k < NB; k++) v |= (int32_t)((w[k] >> s) & 1ull) << k;
-        for (int k = NB; k < nbits; k++) v |= (int32_t)((slices[((size_t)k * n + u) * W + i] >> s) & 1ull) << k;
       }
       dist[(size_t)(64 * i + s) * n + u] = v;
     }
@@ -688,54 +758,54 @@ __device__ __forceinline__ void emit_vertex(int32_t* __restrict__ dist, int32_t 
 
 // Four consecutive vertices u0..u0+3 per thread: every source row gets one
 // 16-byte store, so a warp writes 512 contiguous bytes per row (needs n and
-// the output base 16-byte aligned, which the caller checks).
+// the output base 16-byte aligned, which the caller checks).  Rows holding a
+// pair written during the traversal (see emit_vertex) get scalar stores for
+// the other three.
 template <int W, int NB>
 __device__ __forceinline__ void emit_vertex4(int32_t* __restrict__ dist, int32_t n, int nb_src, size_t u0,
                                              const u64* __restrict__ visit, const u64* __restrict__ slices,
-                                             int nbits) {
+                                             const int32_t* __restrict__ src) {
 #pragma unroll
   for (int i = 0; i < W; i++) {
     if (64 * i >= nb_src) break;
-    u64 vis[4];
-    u64 w[NB > 0 ? NB : 1][4];
+    u64 vis[4], any[4];
+    u64 w[NB][4];
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       vis[j] = visit[(u0 + j) * W + i];
+      any[j] = 0ull;
 #pragma unroll
-      for (int k = 0; k < NB; k++) w[k][j] = slices[((size_t)k * n + u0 + j) * W + i];
+      for (int k = 0; k < NB; k++) {
+        w[k][j] = slices[((size_t)k * n + u0 + j) * W + i];
+        any[j] |= w[k][j];
+      }
     }
     const int cnt = min(64, nb_src - 64 * i);
     for (int s = 0; s < cnt; s++) {
       int32_t v[4];
+      bool keep[4];
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         v[j] = -1;
+        keep[j] = false;
         if ((vis[j] >> s) & 1ull) {
           int32_t x = 0;
 #pragma unroll
           for (int k = 0; k < NB; k++) x |= (int32_t)((w[k][j] >> s) & 1ull) << k;
-          for (int k = NB; k < nbits; k++)
-            x |= (int32_t)((slices[((size_t)k * n + u0 + j) * W + i] >> s) & 1ull) << k;
           v[j] = x;
+          keep[j] = src && !((any[j] >> s) & 1ull) && src[64 * i + s] != (int32_t)(u0 + j);
         }
       }
-      *reinterpret_cast<int4*>(dist + (size_t)(64 * i + s) * n + u0) = make_int4(v[0], v[1], v[2], v[3]);
+      int32_t* row = dist + (size_t)(64 * i + s) * n + u0;
+      if (!(keep[0] | keep[1] | keep[2] | keep[3])) {
+        *reinterpret_cast<int4*>(row) = make_int4(v[0], v[1], v[2], v[3]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (!keep[j]) row[j] = v[j];
+      }
     }
   }
-}
-
-// 32 x 32 bit transpose across a warp: lane i holds row i on entry and
-// column i on exit (bit j of lane i's result = bit i of lane j's input).
-__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
-  const int lane = lane_id();
-  const uint32_t left[5] = {0x0000FFFFu, 0x00FF00FFu, 0x0F0F0F0Fu, 0x33333333u, 0x55555555u};
-#pragma unroll
-  for (int t = 0; t < 5; t++) {
-    const int s = 16 >> t;
-    const uint32_t y = __shfl_xor_sync(kFull, x, s);
-    x = (lane & s) ? ((x & ~left[t]) | ((y & ~left[t]) >> s)) : ((x & left[t]) | ((y & left[t]) << s));
-  }
-  return x;
 }
 
 // Closeness mode of the final pass: per source of the batch, the sum of its
@@ -790,24 +860,35 @@ __device__ __forceinline__ void emit_closeness(const BsCtl* __restrict__ ctl, co
 
 // Level mode of the final pass (one-word batches): each vertex's levels for
 // the batch's sources as one 64-word row (-1 where unreached), and the
-// lowest and highest level among them (INT_MAX / -1 when none).
+// lowest and highest level among them (INT_MAX / -1 when none).  Entries
+// written during the traversal (src set, as in emit_vertex) are kept.
 template <int W>
 __device__ __forceinline__ void emit_levels(const BsCtl* __restrict__ ctl, const u64* __restrict__ visit,
-                                            const u64* __restrict__ slices, int32_t n, int nb, int nbits) {
+                                            const u64* __restrict__ slices, int32_t n, int nb, int nbits,
+                                            const int32_t* __restrict__ src) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < (size_t)n; u += stride) {
     const u64 vis = visit[u * W];
+    u64 any = 0ull;
+    for (int k = 0; k < nbits; k++) any |= slices[((size_t)k * n + u) * W];
     int lo = 0x7fffffff, hi = -1;
     int4* row = reinterpret_cast<int4*>(ctl->lv_block + u * 64);
     for (int s0 = 0; s0 < 64; s0 += 4) {
       int32_t v[4];
+      int4 old = make_int4(0, 0, 0, 0);
+      if (src && (vis & ~any & (0xfull << s0))) old = row[s0 / 4];
+      const int32_t kept[4] = {old.x, old.y, old.z, old.w};
 #pragma unroll
       for (int j = 0; j < 4; j++) {
         const int s = s0 + j;
         v[j] = -1;
         if (s < nb && ((vis >> s) & 1ull)) {
           int32_t x = 0;
-          for (int k = 0; k < nbits; k++) x |= (int32_t)((slices[((size_t)k * n + u) * W] >> s) & 1ull) << k;
+          if (src && !((any >> s) & 1ull) && src[s] != (int32_t)u) {
+            x = kept[j];
+          } else {
+            for (int k = 0; k < nbits; k++) x |= (int32_t)((slices[((size_t)k * n + u) * W] >> s) & 1ull) << k;
+          }
           v[j] = x;
           lo = min(lo, x);
           hi = max(hi, x);
@@ -823,46 +904,41 @@ __device__ __forceinline__ void emit_levels(const BsCtl* __restrict__ ctl, const
 template <int W>
 __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__ ctl, const u64* __restrict__ visit,
                                                        const u64* __restrict__ slices, int32_t n) {
-  if (ctl->lv_block) {
-    if (W == 1)
-      emit_levels<W>(ctl, visit, slices, n, min(64, ctl->nsrc - ctl->batch * 64), 32 - __clz(max(ctl->level, 1)));
-    return;
-  }
-  if (ctl->cc_sum) {
-    const int per = 64 * W;
-    emit_closeness<W>(ctl, visit, slices, n, min(per, ctl->nsrc - ctl->batch * per),
-                      32 - __clz(max(ctl->level, 1)));
-    return;
-  }
   const int batch = ctl->batch;
   const int per = 64 * W;
   const int nb = min(per, ctl->nsrc - batch * per);
-  const int nbits = 32 - __clz(max(ctl->level, 1));
+  // levels below kDeepLevel are in the slices; deeper ones were written out
+  const int nbits = min(32 - __clz(max(ctl->level, 1)), kShallowBits);
+  const int32_t* src = ctl->level >= kDeepLevel ? ctl->sources + (size_t)batch * per : nullptr;
+  if (ctl->lv_block) {
+    if (W == 1) emit_levels<W>(ctl, visit, slices, n, min(64, ctl->nsrc - batch * 64), nbits, src);
+    return;
+  }
+  if (ctl->cc_sum) {
+    emit_closeness<W>(ctl, visit, slices, n, nb, nbits);
+    return;
+  }
   int32_t* dist = ctl->dist_base + (size_t)batch * per * n;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   if ((n & 3) == 0 && (reinterpret_cast<uintptr_t>(dist) & 15) == 0) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)n / 4; q += stride) {
       switch (nbits) {
-        case 1: emit_vertex4<W, 1>(dist, n, nb, 4 * q, visit, slices, nbits); break;
-        case 2: emit_vertex4<W, 2>(dist, n, nb, 4 * q, visit, slices, nbits); break;
-        case 3: emit_vertex4<W, 3>(dist, n, nb, 4 * q, visit, slices, nbits); break;
-        case 4: emit_vertex4<W, 4>(dist, n, nb, 4 * q, visit, slices, nbits); break;
-        case 5: emit_vertex4<W, 5>(dist, n, nb, 4 * q, visit, slices, nbits); break;
-        default: emit_vertex4<W, 6>(dist, n, nb, 4 * q, visit, slices, nbits); break;
+        case 1: emit_vertex4<W, 1>(dist, n, nb, 4 * q, visit, slices, src); break;
+        case 2: emit_vertex4<W, 2>(dist, n, nb, 4 * q, visit, slices, src); break;
+        case 3: emit_vertex4<W, 3>(dist, n, nb, 4 * q, visit, slices, src); break;
+        case 4: emit_vertex4<W, 4>(dist, n, nb, 4 * q, visit, slices, src); break;
+        default: emit_vertex4<W, 5>(dist, n, nb, 4 * q, visit, slices, src); break;
       }
     }
     return;
   }
   for (size_t u = blockIdx.x * (size_t)blockDim.x + threadIdx.x; u < (size_t)n; u += stride) {
     switch (nbits) {
-      case 1: emit_vertex<W, 1>(dist, n, nb, u, visit, slices, nbits); break;
-      case 2: emit_vertex<W, 2>(dist, n, nb, u, visit, slices, nbits); break;
-      case 3: emit_vertex<W, 3>(dist, n, nb, u, visit, slices, nbits); break;
-      case 4: emit_vertex<W, 4>(dist, n, nb, u, visit, slices, nbits); break;
-      case 5: emit_vertex<W, 5>(dist, n, nb, u, visit, slices, nbits); break;
-      case 6: emit_vertex<W, 6>(dist, n, nb, u, visit, slices, nbits); break;
-      case 7: emit_vertex<W, 7>(dist, n, nb, u, visit, slices, nbits); break;
-      default: emit_vertex<W, 8>(dist, n, nb, u, visit, slices, nbits); break;
+      case 1: emit_vertex<W, 1>(dist, n, nb, u, visit, slices, src); break;
+      case 2: emit_vertex<W, 2>(dist, n, nb, u, visit, slices, src); break;
+      case 3: emit_vertex<W, 3>(dist, n, nb, u, visit, slices, src); break;
+      case 4: emit_vertex<W, 4>(dist, n, nb, u, visit, slices, src); break;
+      default: emit_vertex<W, 5>(dist, n, nb, u, visit, slices, src); break;
     }
   }
 }
@@ -871,7 +947,7 @@ __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__
 // the next level's variant: the forced one if set, else the learned
 // selector if weights are loaded, else push while
 // push_ratio x frontier edges < unfinished in-edges, dense once the
-// frontier's edges reach n / 16.
+// frontier's edges reach n.
 __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, const float* __restrict__ sel_w,
                           cudaGraphConditionalHandle loop, int in_graph) {
   const int lane = threadIdx.x;
@@ -917,9 +993,11 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, const float* __res
   }
   int variant;
   if (policy == DAWN_VARIANT_PUSH || mf * ratio < mu) {
-    // A push whose frontier edges reach n/16 touches enough vertices that a
-    // dense update sweep beats queueing every first touch.
-    variant = mf * 16 >= (long long)n ? kVarDense : kVarPush;
+    // A push whose frontier edges reach n touches enough vertices that a
+    // dense update sweep beats queueing every first touch (at n/16 the
+    // sweeps of a 2048x2048 grid cost 35% more than the lists, and 6% more
+    // on a kNN graph at n/1.5).
+    variant = mf >= (long long)n ? kVarDense : kVarPush;
   } else {
     variant = kVarPull;
   }
@@ -1059,7 +1137,8 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   DAWN_CHECK(build_static_list(g));
   // words (per vertex W each): visit | fr[3] | nxt | level slices[nbits]
   // lists: aq[3] | tq | ul[2] | touched bitmap ; segments[3]
-  const int nbits = 32 - __builtin_clz((unsigned)n);  // levels never exceed n
+  // Levels never exceed n, and levels from kDeepLevel on bypass the slices.
+  const int nbits = std::min(32 - __builtin_clz((unsigned)n), kShallowBits);
   // The cached graphs hold the word buffer's address: a wider batch that
   // grows the buffer makes the narrower widths' graphs stale.
   const void* words_before = g->bs_words.p;

@@ -254,3 +254,26 @@ def test_small_levels_change_nothing():
         assert st_on.edges_traversed == st_off.edges_traversed == edges
         assert st_on.levels == st_off.levels
         assert st_on.push_levels + st_on.pull_levels == st_off.push_levels + st_off.pull_levels
+
+
+@pytest.mark.parametrize("width", [1, 2, 4])
+def test_deep_levels_written_directly(width):
+    # past level 32 the batched traversal writes new (source, vertex) pairs
+    # out at once and the final pass keeps them: a grid (diameter 98) and a
+    # directed path (levels up to 599) at every batch width, with ragged last
+    # batches, duplicate sources and a source sitting at the far end; the
+    # forced variants take the pull and dense paths past level 32 as well
+    grid = gen.grid(40, 60)
+    gsrc = np.concatenate([gen.sources(grid, 150, seed=61), [0, 0, grid.n - 1]]).astype(np.int32)
+    path = directed_path(600)
+    psrc = np.array([0, 1, 300, 599, 5], np.int32)
+    for g, srcs in ((grid, gsrc), (path, psrc)):
+        want, edges = expected(g, srcs)
+        with abi.Graph(g) as dg:
+            dg.set_option(abi.OPT_BITSET_WIDTH, width)
+            for force in (0, 1, 2, 3):
+                dg.set_option(abi.OPT_FORCE_VARIANT, force)
+                d, st = dg.bfs(srcs, variant=abi.VARIANT_BITSET)
+                bad = np.argwhere(d != want)
+                assert bad.size == 0, (g.n, width, force, bad[:5])
+                assert st.edges_traversed == edges

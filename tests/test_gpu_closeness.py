@@ -62,3 +62,20 @@ def test_closeness_high_diameter():
     with abi.Graph(g) as dg:
         cc, _, _ = dg.closeness(srcs)
     np.testing.assert_allclose(cc, want, rtol=RTOL, atol=0)
+
+
+@pytest.mark.parametrize("width", [1, 4])
+def test_closeness_deep_levels_many_sources(width):
+    # every vertex of a grid a source: most pairs are reached past level 32,
+    # where the sums are added level by level during the traversal
+    g = gen.grid(12, 40)
+    srcs = np.arange(g.n, dtype=np.int32)
+    ref, _, _ = O.mssp(g, srcs)
+    want = np.array([O.closeness_hops(ref[i], s) for i, s in enumerate(srcs)])
+    api = O.hops_ref_to_api(ref, srcs)
+    with abi.Graph(g) as dg:
+        dg.set_option(abi.OPT_BITSET_WIDTH, width)
+        cc, sums, reached = dg.closeness(srcs)
+    np.testing.assert_allclose(cc, want, rtol=RTOL, atol=0)
+    assert np.array_equal(reached, (api > 0).sum(axis=1))
+    assert np.array_equal(sums, np.where(api > 0, api, 0).sum(axis=1).astype(np.float64))
