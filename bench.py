@@ -281,9 +281,9 @@ def suite_lines(torch, abi, gen, stream, rank):
     """The other workload shapes, one JSON line each (not the headline line):
     directed ER n=65,536 x 64 sources (the CPU-runnable case), weighted
     SSSP on the RMAT-22 topology x 64 sources (int32 and float32 weights),
-    RMAT-18 x 4,096 sources, and 512 uneven directed ER graphs (n in
+    RMAT-18 x 4,096 sources, 512 uneven directed ER graphs (n in
     [1,024, 65,536], average degree in [4, 32], 8-64 sources each) in one
-    persistent launch."""
+    persistent launch, BCDAWN betweenness, and two high-diameter graphs."""
     out = []
 
     def timed(fn, steps=3):
@@ -384,6 +384,29 @@ def suite_lines(torch, abi, gen, stream, rank):
                 tot_edges += st.edges_traversed
         out.append({"suite": "er512-multi-graph-bfs", "variant": f"{name} (first {sub} graphs)",
                     "ms_per_step": round(tot_ms, 3), "gteps": round(tot_edges / (tot_ms * 1e-3) / 1e9, 2)})
+    # high-diameter shapes: a 2048 x 2048 4-neighbour grid and a k = 8 kNN
+    # graph on 2^21 uniform points; single-source traversals with the small-
+    # frontier cluster levels on and off, and the batched traversal (levels
+    # from 32 on written out directly)
+    for name, g in (("grid2048x2048", gen.grid(2048, 2048)), ("knn2M-k8", gen.knn(1 << 21, 8, seed=GRAPH_SEED))):
+        srcs = gen.sources(g, NSRC, seed=SOURCE_SEED)
+        with abi.Graph(g, stream=stream) as dg:
+            d = torch.empty((NSRC, g.n), dtype=torch.int32, device="cuda")
+            for small in (1, 0):
+                dg.set_option(abi.OPT_SMALL_LEVELS, small)
+                st = dg.bfs_device(srcs[:2], d.data_ptr(), variant=abi.VARIANT_DO)
+                ms = timed(lambda: dg.bfs_device(srcs[:2], d.data_ptr(), variant=abi.VARIANT_DO, stats=False), 1)
+                out.append({"suite": f"{name}-bfs", "variant": "single-source, small-frontier cluster levels "
+                            + ("on" if small else "off"), "ms_per_source": round(ms / 2, 3),
+                            "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 3), "levels": st.levels // 2,
+                            "n": g.n, "m": g.m})
+            dg.set_option(abi.OPT_SMALL_LEVELS, 1)
+            st = dg.bfs_device(srcs, d.data_ptr(), variant=abi.VARIANT_BITSET)
+            ms = timed(lambda: dg.bfs_device(srcs, d.data_ptr(), variant=abi.VARIANT_BITSET, stats=False), 2)
+            out.append({"suite": f"{name}-bfs", "variant": f"batched bitset, {NSRC} sources",
+                        "ms_per_step": round(ms, 3), "ms_per_source": round(ms / NSRC, 3),
+                        "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 3), "levels": st.levels})
+        del g, d
     if rank == 0:
         for line in out:
             print(json.dumps(line), flush=True)
