@@ -154,13 +154,17 @@ __host__ __device__ inline size_t seg_capacity(int32_t n, long long m) {
   return 2 * (size_t)(m / kSeg) + 64;
 }
 
-// The whole warp writes the segments of every lane in lm (nseg segments
-// of lane l's row from CSR position rs, at list index first): a hub's
-// thousands of segments go out 32 per store instead of one lane writing
-// them all.
+// Writes the segments of every lane in lm (nseg segments of lane l's row
+// from CSR position rs, at list index first).  A lane writes up to
+// kOwnSegs of its own; the whole warp writes a longer row's, so a hub's
+// thousands of segments go out 32 per store instead of from one lane.
+constexpr int kOwnSegs = 16;
 __device__ __forceinline__ void write_segments(uint32_t lm, int32_t u, int rs, int nseg, uint32_t first,
                                                Seg* __restrict__ segs) {
   const int lane = lane_id();
+  if (nseg <= kOwnSegs)
+    for (int j = 0; j < nseg; j++) segs[first + j] = Seg{u, rs + j * kSeg};
+  lm &= __ballot_sync(kFull, nseg > kOwnSegs);
   while (lm) {
     const int l = __ffs(lm) - 1;
     lm &= lm - 1;
