@@ -140,7 +140,8 @@ void destroy(dawn_graph* g) {
                     &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
                     &g->dist_stage, &g->pt_voff, &g->pt_tasks, &g->pt_sources, &g->pt_ctl, &g->pt_scratch, &g->pt_rows,
                     &g->sel_slot, &g->wt_col, &g->wt_val, &g->mw_block, &g->mw_masks,
-                    &g->mw_ctl, &g->mw_sources, &g->bc_levels, &g->bc_terms, &g->bc_range, &g->bc_out};
+                    &g->mw_ctl, &g->mw_sources, &g->bc_levels, &g->bc_terms, &g->bc_range, &g->bc_out,
+                    &g->bc_heavy, &g->bc_part};
   for (DevBuf* b : bufs) dawn::release(*b);
   if (g->stream) cudaStreamSynchronize(g->stream);
   if (g->bfs_exec) cudaGraphExecDestroy(g->bfs_exec);

@@ -187,6 +187,9 @@ struct dawn_graph {
   dawn::DevBuf bc_terms;    // n x 64 float (1 / amount + dependency)
   dawn::DevBuf bc_range;    // 2 x n int32 lowest / highest level per vertex
   dawn::DevBuf bc_out;      // n double (host-pointer calls)
+  dawn::DevBuf bc_heavy;    // rows cut into segments: out-rows (ids, segment prefix), in-rows (same)
+  dawn::DevBuf bc_part;     // per-segment partial sums (float) / per-heavy-row counts (int32), 64 each
+  int32_t bc_hout = -1, bc_segs_out = 0, bc_hin = 0, bc_segs_in = 0;  // -1: lists not built
   dawn::DevBuf mw_block;    // batched weighted traversal: n x 64 int32 distances
   dawn::DevBuf mw_masks;    // 3 x n uint64 improved-source masks
   dawn::DevBuf mw_ctl;

@@ -54,3 +54,18 @@ def test_source_subsets():
         with abi.Graph(small) as dg:
             got, _ = dg.betweenness()
         np.testing.assert_allclose(got, O.ref_bc(small).astype(np.float64), rtol=RTOL, atol=1e-3)
+
+
+def test_heavy_rows_in_segments():
+    # hubs of more than 128 entries: their rows are cut into 64-entry
+    # segments in both the amount pass and the sweeps; several batches so
+    # the per-row counters are reused; directed too (in-rows differ)
+    g = gen.rmat(12, 16, a=0.65, b=0.15, c=0.15, seed=96)
+    assert g.degrees().max() > 1100
+    check(g, gen.sources(g, 200, seed=97))
+    d = gen.rmat(12, 16, a=0.65, b=0.15, c=0.15, seed=98)
+    tail = np.repeat(np.arange(d.n), np.diff(d.row_ptr))
+    keep = (tail * 7 + d.col) % 3 != 0  # drops one direction of many pairs
+    rp = np.concatenate([[0], np.cumsum(np.bincount(tail[keep], minlength=d.n))]).astype(np.int32)
+    directed = gen.CsrGraph(d.n, rp, d.col[keep].astype(np.int32))
+    check(directed, np.arange(0, d.n, 37, dtype=np.int32))
