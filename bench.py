@@ -429,6 +429,9 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner before the timed steps")
     ap.add_argument("--variant", default="bitset", choices=["bitset", "learned", "do", "push", "sssp", "sssp-single"],
                     help="--quick only: the traversal to run (sssp: batched weighted, int32 weights)")
+    ap.add_argument("--graph", default="rmat", choices=["rmat", "grid1024", "grid2048", "knn2M"],
+                    help="--quick only: rmat (of --scale), a 4-neighbour grid, or a k = 8 kNN graph on 2^21 points")
+    ap.add_argument("--sources", type=int, default=NSRC, help="--quick only: sources per step")
     ap.add_argument("--suite", action="store_true",
                     help="also time the other workload shapes (one JSON line each, before the main line)")
     args = ap.parse_args()
@@ -449,7 +452,15 @@ def main():
         _s = torch.cuda.Stream()
         torch.cuda.set_stream(_s)
         suite_lines(torch, abi, _gen, _s.cuda_stream, rank)
-    g, srcs = make_workload(args.scale, rank, weighted=args.quick and args.variant.startswith("sssp"))
+    if args.quick and args.graph != "rmat":
+        from dawn_gb300 import gen as _gen
+        g = {"grid1024": lambda: _gen.grid(1024, 1024), "grid2048": lambda: _gen.grid(2048, 2048),
+             "knn2M": lambda: _gen.knn(1 << 21, 8, seed=GRAPH_SEED)}[args.graph]()
+        srcs = _gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
+    else:
+        g, srcs = make_workload(args.scale, rank, weighted=args.quick and args.variant.startswith("sssp"))
+    if args.quick:
+        srcs = srcs[:args.sources]
     # A dedicated stream: the library launches on it and torch's events
     # record on it (the legacy default stream has handle 0, which the C ABI
     # reads as "library-owned stream").
@@ -489,7 +500,8 @@ def main():
         dg.trace(False)
         st = run(True)
         if rank == 0:
-            print(json.dumps({"quick": True, "variant": args.variant, "traced": args.traced, "scale": args.scale,
+            print(json.dumps({"quick": True, "variant": args.variant, "traced": args.traced, "graph": args.graph,
+                              "scale": args.scale, "sources": len(srcs),
                               "ms_per_step": round(ms, 4), "edges": st.edges_traversed,
                               "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2),
                               "kernels": len(recs)}), flush=True)
