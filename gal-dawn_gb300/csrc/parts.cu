@@ -40,7 +40,7 @@ namespace dawn {
 namespace {
 
 using u64 = unsigned long long;
-constexpr int kPartBlock = 512;
+constexpr int kPartBlock = 1024;
 constexpr int kPartSlices = 8;  // level slices kept in registers by the emit pass
 
 struct PartsCtl {
@@ -113,7 +113,7 @@ __device__ __forceinline__ void emit_part_vertex(int32_t* __restrict__ dist, int
   for (int k = NB; k < nbits; k++) slices[(size_t)k * maxn + u] = 0ull;
 }
 
-__global__ void __launch_bounds__(kPartBlock, 2) parts_traverse(PartsCtl* __restrict__ ctl,
+__global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __restrict__ ctl,
                                                            const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ col,
                                                            const int32_t* __restrict__ t_row_ptr,
