@@ -14,7 +14,9 @@
 //     slots rotate by level % 3: level L reads (L-1)%3, writes L%3, clears
 //     (L+1)%3);
 //   * a warp takes one frontier vertex (rows of >= 128 entries one
-//     128-entry segment at a time); lane i owns sources i and i + 32.  The
+//     128-entry segment at a time), or, for vertices active for at most
+//     kSparse sources, a lane takes one (vertex, source) pair; in the warp
+//     form lane i owns sources i and i + 32.  The
 //     warp loads 32 of the row's targets and weights in one coalesced read,
 //     then for each edge every lane relaxes its two sources against the
 //     target's distance row (fetched for four edges at a time) and issues a
@@ -114,9 +116,102 @@ __global__ void __launch_bounds__(1024) mw_init(MwCtl* __restrict__ ctl, const i
   if (threadIdx.x == 0) ctl->done = ctl->qsize[0] == 0 && ctl->lpack[0] == 0;
 }
 
-// One level.  Warp tasks: the long-row segments, then the short-row
-// vertices of the input queue (grid-stride over warps).
-__global__ void __launch_bounds__(kBlock, 5) mw_push(const int32_t* __restrict__ row_ptr,
+// The row [k0, k1) of frontier vertex u relaxed by one warp: lane i owns
+// sources i and i + 32 of the batch.  The warp loads 32 targets and weights
+// in one coalesced read; for each edge every lane relaxes its two sources
+// against the target's distance row (fetched for kUnroll edges at a time)
+// and issues a return-free atomicMin where it improves on the fetched
+// value.  Lane j collects the improved sources of edge kb + j, so the
+// next-mask update and the queue append run once per 32 edges.  All 32
+// lanes call it with the same arguments.
+__device__ __forceinline__ void relax_row(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                                          const int32_t* __restrict__ w, bool fl, int32_t* __restrict__ D,
+                                          unsigned long long* __restrict__ m_out, int32_t u, int k0, int k1,
+                                          unsigned long long mask, WarpQueue& wq, Seg* __restrict__ sout,
+                                          unsigned long long* lpack, unsigned long long& my_mf) {
+  const int lane = lane_id();
+  const bool actA = (mask >> lane) & 1ull, actB = (mask >> (lane + 32)) & 1ull;
+  const int32_t* du = D + (size_t)u * kBatch;
+  const int32_t dA = __ldcg(du + lane), dB = __ldcg(du + lane + 32);
+  for (int kb = k0; kb < k1; kb += 32) {
+    const int k = kb + lane;
+    const int32_t cv = k < k1 ? __ldg(col + k) : -1;
+    const int32_t cw = k < k1 ? __ldg(w + k) : 0;
+    const int cnt = min(32, k1 - kb);
+    unsigned long long mybits = 0ull;
+    for (int j0 = 0; j0 < cnt; j0 += kUnroll) {
+      int32_t v[kUnroll], wv[kUnroll], curA[kUnroll], curB[kUnroll];
+#pragma unroll
+      for (int i = 0; i < kUnroll; i++) {
+        v[i] = __shfl_sync(kFull, cv, (j0 + i) & 31);
+        wv[i] = __shfl_sync(kFull, cw, (j0 + i) & 31);
+        if (j0 + i >= cnt) v[i] = -1;
+      }
+#pragma unroll
+      for (int i = 0; i < kUnroll; i++) {
+        const int32_t* dv = D + (size_t)(v[i] < 0 ? 0 : v[i]) * kBatch;
+        curA[i] = (v[i] >= 0 && actA) ? __ldcg(dv + lane) : 0;
+        curB[i] = (v[i] >= 0 && actB) ? __ldcg(dv + lane + 32) : 0;
+      }
+      bool impA[kUnroll], impB[kUnroll];
+#pragma unroll
+      for (int i = 0; i < kUnroll; i++) {
+        impA[i] = impB[i] = false;
+        if (v[i] < 0) continue;
+        int32_t* dv = D + (size_t)v[i] * kBatch;
+        // Improvement is judged against the row fetched above and the
+        // minimum is a reduction without a return value: a target whose
+        // entry another warp lowered further in the meantime is only
+        // relaxed once more at the next level, which leaves the fixed
+        // point unchanged.
+        if (actA) {
+          const int32_t c = relax(dA, wv[i], fl);
+          if (c < curA[i]) {
+            atomicMin(dv + lane, c);
+            impA[i] = true;
+          }
+        }
+        if (actB) {
+          const int32_t c = relax(dB, wv[i], fl);
+          if (c < curB[i]) {
+            atomicMin(dv + lane + 32, c);
+            impB[i] = true;
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kUnroll; i++) {
+        const unsigned long long bits = (unsigned long long)__ballot_sync(kFull, impA[i]) |
+                                        ((unsigned long long)__ballot_sync(kFull, impB[i]) << 32);
+        if (lane == j0 + i) mybits = bits;
+      }
+    }
+    bool first = false;
+    int deg = 0, rs = 0;
+    if (mybits) {
+      first = atomicOr(m_out + cv, mybits) == 0ull;
+      if (first) {
+        rs = row_ptr[cv];
+        deg = row_ptr[cv + 1] - rs;
+        my_mf += (unsigned long long)deg;
+      }
+    }
+    emit_routed(first, cv, deg, rs, wq, sout, lpack);
+  }
+}
+
+// Frontier vertices whose mask holds at most kSparse sources (the waves of
+// different sources crossing a high-diameter graph: most vertices are
+// active for one or two of the 64 at a time) go through pairs instead of a
+// warp per vertex: one lane per (vertex, improved source), relaxing that
+// source along the vertex's row with kUnroll targets in flight.
+constexpr int kSparse = 8;
+
+// One level.  Warp tasks: the long-row segments (a warp each), then the
+// input queue 32 vertices at a time: the vertices with dense masks get the
+// warp one after another, the sparse ones are dealt as (vertex, source)
+// pairs across the lanes.
+__global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__ row_ptr,
                                                   const int32_t* __restrict__ col, const int32_t* __restrict__ w,
                                                   int is_float, MwCtl* __restrict__ ctl, int32_t* __restrict__ D,
                                                   unsigned long long* __restrict__ masks, int32_t* __restrict__ q,
@@ -136,6 +231,7 @@ __global__ void __launch_bounds__(kBlock, 5) mw_push(const int32_t* __restrict__
   const Seg* sin = segs + (size_t)pin * segcap;
   const int qn = ctl->qsize[pin];
   const int ln = seg_count(ctl->lpack[pin]);
+  const int ngroups = (qn + 31) / 32;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   const bool fl = is_float != 0;
   WarpQueue wq(s_q[wib], q + (size_t)pout * n, &ctl->qsize[pout]);
@@ -143,91 +239,88 @@ __global__ void __launch_bounds__(kBlock, 5) mw_push(const int32_t* __restrict__
   unsigned long long* lpack = &ctl->lpack[pout];
   unsigned long long my_mf = 0;
 
-  for (int t = global_warp(); t < ln + qn; t += num_warps()) {
-    int32_t u;
-    int k0, k1;
+  for (int t = global_warp(); t < ln + ngroups; t += num_warps()) {
     if (t < ln) {
       const Seg sg = sin[t];
-      u = sg.v;
-      k0 = sg.k0;
-      k1 = min(k0 + kSeg, row_ptr[u + 1]);
-    } else {
-      u = qin[t - ln];
+      const int k1 = min(sg.k0 + kSeg, row_ptr[sg.v + 1]);
+      relax_row(row_ptr, col, w, fl, D, m_out, sg.v, sg.k0, k1, __ldcg(m_in + sg.v), wq, sout, lpack, my_mf);
+      continue;
+    }
+    const int i = (t - ln) * 32 + lane;
+    int32_t u = -1;
+    int k0 = 0, k1 = 0;
+    unsigned long long mask = 0ull;
+    if (i < qn) {
+      u = qin[i];
       k0 = row_ptr[u];
       k1 = row_ptr[u + 1];
+      mask = __ldcg(m_in + u);
     }
-    const unsigned long long mask = __ldcg(m_in + u);
-    const bool actA = (mask >> lane) & 1ull, actB = (mask >> (lane + 32)) & 1ull;
-    const int32_t* du = D + (size_t)u * kBatch;
-    const int32_t dA = __ldcg(du + lane), dB = __ldcg(du + lane + 32);
-    for (int kb = k0; kb < k1; kb += 32) {
-      const int k = kb + lane;
-      const int32_t cv = k < k1 ? __ldg(col + k) : -1;
-      const int32_t cw = k < k1 ? __ldg(w + k) : 0;
-      const int cnt = min(32, k1 - kb);
-      // Lane j collects the improved sources of edge kb + j (its own edge),
-      // so the next-mask update and the queue append run once per 32 edges.
-      unsigned long long mybits = 0ull;
-      // kUnroll edges at a time: their distance rows are all loaded, then
-      // all atomics issued, before the first ballot
-      for (int j0 = 0; j0 < cnt; j0 += kUnroll) {
-        int32_t v[kUnroll], wv[kUnroll], curA[kUnroll], curB[kUnroll];
+    const int pc = __popcll(mask);
+    const bool sparse = pc <= kSparse;
+    uint32_t dense = __ballot_sync(kFull, !sparse);
+    while (dense) {
+      const int l = __ffs(dense) - 1;
+      dense &= dense - 1;
+      relax_row(row_ptr, col, w, fl, D, m_out, __shfl_sync(kFull, u, l), __shfl_sync(kFull, k0, l),
+                __shfl_sync(kFull, k1, l), __shfl_sync(kFull, mask, l), wq, sout, lpack, my_mf);
+    }
+    // (vertex, source) pairs of the sparse lanes, 32 at a time
+    const int np = sparse && k1 > k0 ? pc : 0;
+    const int incl = warp_incl_scan(np);
+    const int excl = incl - np;
+    const int total = __shfl_sync(kFull, incl, 31);
+    for (int e0 = 0; e0 < total; e0 += 32) {
+      const int e = e0 + lane;
+      int lo = 0;  // last lane whose first pair is <= e
 #pragma unroll
-        for (int i = 0; i < kUnroll; i++) {
-          v[i] = __shfl_sync(kFull, cv, (j0 + i) & 31);
-          wv[i] = __shfl_sync(kFull, cw, (j0 + i) & 31);
-          if (j0 + i >= cnt) v[i] = -1;
+      for (int step = 16; step; step >>= 1) {
+        const int ex = __shfl_sync(kFull, excl, lo + step);
+        if (ex <= e) lo += step;
+      }
+      const bool ok = e < total;
+      const int r = e - __shfl_sync(kFull, excl, lo);
+      unsigned long long m = __shfl_sync(kFull, mask, lo);
+      const int32_t pu = __shfl_sync(kFull, u, lo);
+      const int pk0 = __shfl_sync(kFull, k0, lo), pk1 = __shfl_sync(kFull, k1, lo);
+      int src = 0, nd = 0;
+      int32_t dsu = 0;
+      if (ok) {
+        for (int c = 0; c < r; c++) m &= m - 1;  // drop the r lowest sources
+        src = __ffsll((long long)m) - 1;
+        dsu = __ldcg(D + (size_t)pu * kBatch + src);
+        nd = pk1 - pk0;
+      }
+      const int maxd = (int)__reduce_max_sync(kFull, (unsigned)nd);
+      for (int j0 = 0; j0 < maxd; j0 += kUnroll) {
+        int32_t v[kUnroll], wv[kUnroll], cur[kUnroll];
+#pragma unroll
+        for (int x = 0; x < kUnroll; x++) {
+          const bool act = j0 + x < nd;
+          v[x] = act ? __ldg(col + pk0 + j0 + x) : -1;
+          wv[x] = act ? __ldg(w + pk0 + j0 + x) : 0;
         }
 #pragma unroll
-        for (int i = 0; i < kUnroll; i++) {
-          const int32_t* dv = D + (size_t)(v[i] < 0 ? 0 : v[i]) * kBatch;
-          curA[i] = (v[i] >= 0 && actA) ? __ldcg(dv + lane) : 0;
-          curB[i] = (v[i] >= 0 && actB) ? __ldcg(dv + lane + 32) : 0;
-        }
-        bool impA[kUnroll], impB[kUnroll];
+        for (int x = 0; x < kUnroll; x++) cur[x] = v[x] >= 0 ? __ldcg(D + (size_t)v[x] * kBatch + src) : 0;
 #pragma unroll
-        for (int i = 0; i < kUnroll; i++) {
-          impA[i] = impB[i] = false;
-          if (v[i] < 0) continue;
-          int32_t* dv = D + (size_t)v[i] * kBatch;
-          // Improvement is judged against the row fetched above and the
-          // minimum is a reduction without a return value: a target whose
-          // entry another warp lowered further in the meantime is only
-          // relaxed once more at the next level, which leaves the fixed
-          // point unchanged.
-          if (actA) {
-            const int32_t c = relax(dA, wv[i], fl);
-            if (c < curA[i]) {
-              atomicMin(dv + lane, c);
-              impA[i] = true;
+        for (int x = 0; x < kUnroll; x++) {
+          bool first = false;
+          int deg = 0, rs = 0;
+          if (v[x] >= 0) {
+            const int32_t c = relax(dsu, wv[x], fl);
+            if (c < cur[x]) {
+              atomicMin(D + (size_t)v[x] * kBatch + src, c);
+              first = atomicOr(m_out + v[x], 1ull << src) == 0ull;
+              if (first) {
+                rs = row_ptr[v[x]];
+                deg = row_ptr[v[x] + 1] - rs;
+                my_mf += (unsigned long long)deg;
+              }
             }
           }
-          if (actB) {
-            const int32_t c = relax(dB, wv[i], fl);
-            if (c < curB[i]) {
-              atomicMin(dv + lane + 32, c);
-              impB[i] = true;
-            }
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < kUnroll; i++) {
-          const unsigned long long bits = (unsigned long long)__ballot_sync(kFull, impA[i]) |
-                                          ((unsigned long long)__ballot_sync(kFull, impB[i]) << 32);
-          if (lane == j0 + i) mybits = bits;
+          emit_routed(first, v[x], deg, rs, wq, sout, lpack);
         }
       }
-      bool first = false;
-      int deg = 0, rs = 0;
-      if (mybits) {
-        first = atomicOr(m_out + cv, mybits) == 0ull;
-        if (first) {
-          rs = row_ptr[cv];
-          deg = row_ptr[cv + 1] - rs;
-          my_mf += (unsigned long long)deg;
-        }
-      }
-      emit_routed(first, cv, deg, rs, wq, sout, lpack);
     }
   }
   wq.flush();

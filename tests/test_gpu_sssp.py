@@ -157,3 +157,13 @@ def test_batched_directed_asymmetric():
     g = asym_weights(gen.erdos_renyi(5000, 60000, seed=73), 74)
     g = gen.CsrGraph(g.n, g.row_ptr, g.col, g.w_i32, g.w_f32, symmetric=False)
     check(g, gen.sources(g, 70, seed=75, from_lcc=False))
+
+
+def test_batched_high_diameter_sparse_masks():
+    # a weighted grid and a kNN graph, 100 sources: most frontier vertices
+    # are active for a few sources at a time, so the relaxations run as
+    # (vertex, source) pairs; a hub row mixes in the warp-per-vertex form
+    g = gen.grid(40, 60, seed=76, weights=True)
+    check(g, gen.sources(g, 100, seed=77))
+    k = gen.knn(3000, 6, seed=78, weights=True)
+    check(k, gen.sources(k, 70, seed=79))
