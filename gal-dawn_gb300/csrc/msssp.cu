@@ -205,7 +205,7 @@ __device__ __forceinline__ void relax_row(const int32_t* __restrict__ row_ptr, c
 // active for one or two of the 64 at a time) go through pairs instead of a
 // warp per vertex: one lane per (vertex, improved source), relaxing that
 // source along the vertex's row with kUnroll targets in flight.
-constexpr int kSparse = 8;
+constexpr int kSparse = 16;
 
 // One level.  Warp tasks: the long-row segments (a warp each), then the
 // input queue 32 vertices at a time: the vertices with dense masks get the
