@@ -19,6 +19,7 @@
 #include <climits>
 #include <mutex>
 
+#include "cluster_levels.cuh"
 #include "dawn_device.cuh"
 #include "selector.cuh"
 
@@ -27,16 +28,6 @@ namespace {
 
 constexpr long long kAlpha = 14, kBeta = 24;
 
-// Small-frontier levels (bfs_small): one cluster of kSmallCtas CTAs runs
-// push levels back to back while the frontier stays within kSmallFrontier
-// vertices, kSmallEdges out-edges and kSmallCap vertices per CTA, at most
-// kSmallMaxLevels levels per launch.
-constexpr int kSmallCtas = 8;
-constexpr int kSmallBlock = 1024;
-constexpr int kSmallCap = 1536;
-constexpr int kSmallFrontier = 8192;
-constexpr long long kSmallEdges = 32768;
-constexpr int kSmallMaxLevels = 512;
 
 __device__ __forceinline__ uint32_t* rot(uint32_t* fbm, int i, int nwords) {
   return fbm + (size_t)(i % 3) * nwords;
@@ -138,57 +129,6 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }
 
-// Expands one warp batch of frontier rows: lane i holds row (rs, deg) when
-// valid.  Rows of >= kWarpRow entries are swept by the whole warp, shorter
-// ones are concatenated through a warp scan and dealt 32 edges at a time
-// (the owning lane is found by a binary search over the lanes' exclusive
-// offsets, through shuffles).  op(k, valid) runs on all 32 lanes.
-template <class Op>
-__device__ __forceinline__ void expand_rows(bool valid, int rs, int deg, Op&& op) {
-  const int lane = lane_id();
-  if (!valid) deg = 0;
-  uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
-  while (big) {
-    const int leader = __ffs(big) - 1;
-    big &= big - 1;
-    const int s = __shfl_sync(kFull, rs, leader), d = __shfl_sync(kFull, deg, leader);
-    for (int k0 = 0; k0 < d; k0 += 32) op(s + k0 + lane, k0 + lane < d);
-  }
-  const int sdeg = deg < kWarpRow ? deg : 0;
-  const int incl = warp_incl_scan(sdeg);
-  const int excl = incl - sdeg;
-  const int total = __shfl_sync(kFull, incl, 31);
-  for (int e0 = 0; e0 < total; e0 += 32) {
-    const int e = e0 + lane;
-    int lo = 0;  // last lane whose offset is <= e
-#pragma unroll
-    for (int step = 16; step; step >>= 1) {
-      const int ex = __shfl_sync(kFull, excl, lo + step);
-      if (ex <= e) lo += step;
-    }
-    const int k = __shfl_sync(kFull, rs, lo) + (e - __shfl_sync(kFull, excl, lo));
-    op(k, e < total);
-  }
-}
-
-// Rows per warp batch in bfs_small: the level's rows spread over all the
-// cluster's warps (fewer than 32 per warp when the frontier is small), so
-// that each warp's chain of dependent loads is short.
-__device__ __forceinline__ int batch_rows(int rows) {
-  constexpr int kLanes = kSmallCtas * kSmallBlock;
-  if (rows >= kLanes) return 32;
-  const int bs = (rows + kLanes / 32 - 1) / (kLanes / 32);
-  return bs < 1 ? 1 : bs;
-}
-
-// One CTA's share of one level's frontier in bfs_small: discovered vertices
-// with their row start and degree.
-struct SmallSlice {
-  int32_t u[kSmallCap];
-  int32_t rs[kSmallCap];
-  int32_t deg[kSmallCap];
-};
-
 // Small frontiers: a single cluster of kSmallCtas CTAs runs push levels one
 // after another in one launch.
 //   * Each CTA appends the vertices its warps discover to its own shared-
@@ -248,7 +188,7 @@ __global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock
     const int p = L & 1;
     uint32_t my_mf = 0;
     bool my_long = false;
-    auto op = [&](int k, bool valid) {
+    auto op = [&](int k, bool valid, int32_t) {
       const int32_t u = valid ? __ldg(col + k) : -1;
       bool found = false;
       int rs = 0, deg = 0;
@@ -286,7 +226,7 @@ __global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock
       const int pin = p ^ 1;
       const int32_t* qin = q + (size_t)pin * n;
       const int qn = ctl->qsize[pin], ln = seg_count(ctl->lpack[pin]);
-      seg_expand(row_ptr, segs + (size_t)pin * segcap, ln, [&](int32_t, int k, bool valid) { op(k, valid); });
+      seg_expand(row_ptr, segs + (size_t)pin * segcap, ln, [&](int32_t, int k, bool valid) { op(k, valid, 0); });
       const int bs = batch_rows(qn);
       for (int b = cwarp * bs; b < qn; b += kSmallCtas * kWarps * bs) {
         const int i = b + lane;
@@ -297,7 +237,7 @@ __global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock
           rs = row_ptr[v];
           deg = row_ptr[v + 1] - rs;
         }
-        expand_rows(ok, rs, deg, op);
+        expand_rows(ok, rs, deg, 0, op);
       }
     } else {
       // the previous level's slices, across the cluster
@@ -318,7 +258,7 @@ __global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock
           deg = src->deg[off];
           dist[src->u[off]] = L - 1;
         }
-        expand_rows(e < tot, rs, deg, op);
+        expand_rows(e < tot, rs, deg, 0, op);
       }
     }
     my_mf = __reduce_add_sync(kFull, my_mf);
@@ -391,7 +331,7 @@ __global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock
     if (nlev) ctl->prev_nf = last_nf;
     ctl->level = L;
   }
-  cluster.sync();
+  cluster.sync();  // also keeps every CTA resident until no one reads its shared memory
   uint32_t* fcur = rot(fbm, L, nwords);
   const int qn = __ldcg(&ctl->qsize[p]), ln = seg_count(__ldcg(&ctl->lpack[p]));
   for (size_t i = tid; i < (size_t)qn; i += stride) {
@@ -577,7 +517,7 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   c.use_sel = g->sel_call;
   c.sel_margin = g->sel_margin;
   c.force = g->force_variant == 3 ? 1 + kVarPush : g->force_variant;
-  c.small = g->small_levels ? 1 : 0;
+  c.small = g->small_levels && cluster_fits((const void*)bfs_small, kSmallCtas, kSmallBlock) ? 1 : 0;
   c.m = m;
   DAWN_CHECK(upload_ctl(g, c));
 

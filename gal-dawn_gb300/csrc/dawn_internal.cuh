@@ -321,6 +321,10 @@ dawn_status download_ctl(dawn_graph* g, SsCtl* out);
 // CTAs of a persistent grid: the SM count times the resident CTAs per SM,
 // capped at `cap` per SM when cap > 0.
 int persistent_blocks(const void* fn, int block, size_t smem, int cap = 0);
+// Whether one cluster of `ctas` CTAs of `threads` threads of kernel fn (its
+// cluster shape fixed at compile time) can be resident on the current
+// device; the answer is kept per kernel for the process.
+bool cluster_fits(const void* fn, int ctas, int threads);
 dawn_status build_transpose(dawn_graph* g);
 // In-edge tails and weights in the row layout of t_row_ptr (g->wt_col, g->wt_val).
 dawn_status build_weighted_in_edges(dawn_graph* g);

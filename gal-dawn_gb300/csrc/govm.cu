@@ -15,6 +15,8 @@
 //     (src/algorithm/cpu/sssp.cpp:41-46): each distinct neighbour takes the
 //     weight of its last CSR entry, all of them form the first frontier, the
 //     source is set to 0 and is never relaxed afterwards.
+//   * stretches of levels with small frontiers run inside one launch of a
+//     thread-block cluster (sssp_small), as the boolean expand's do;
 //   * levels whose frontier out-edges exceed m run as a pull instead: every vertex with in-edges takes the minimum of d[u] + w over
 //     its in-edges from last level's frontier (a bitmap test per in-edge,
 //     the gathers only for frontier tails), so the dense levels need no
@@ -23,6 +25,10 @@
 // Any relaxation order reaches the same fixed point (the minimum over paths
 // of the path sums, which rounding leaves monotone), so push, pull and
 // their mix give the distances of the reference CPU path.
+#include <cooperative_groups.h>
+#include <climits>
+
+#include "cluster_levels.cuh"
 #include "dawn_device.cuh"
 #include "selector.cuh"
 
@@ -321,7 +327,7 @@ __global__ void __launch_bounds__(kBlock, 6) sssp_step(const int32_t* __restrict
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int32_t s_aux[kBlock / 32][32];
   __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
-  if (ctl->done) return;
+  if (ctl->done || ctl->mode == kModeSmall) return;
   const int wib = threadIdx.x >> 5;
   if (ctl->mode == kModePush)
     push_level(s_excl[wib], s_rs[wib], s_aux[wib], s_q[wib], row_ptr, col, wi, wf, is_float, ctl, q, segs, segcap,
@@ -329,6 +335,198 @@ __global__ void __launch_bounds__(kBlock, 6) sssp_step(const int32_t* __restrict
   else
     pull_level(s_excl[wib], s_rs[wib], s_aux[wib], s_q[wib], row_ptr, t_row_ptr, t_col, t_wi, t_wf, is_float, ctl,
                q, segs, segcap, inq, ul, ul_n, hv, hv_segoff, hv_count, hv_segs, pull_seg, n, nwords);
+}
+
+// Small frontiers, weighted: one cluster runs push levels one after another
+// in one launch, like bfs_small.  A level relaxes the rows of the previous
+// level's slices (each row with its vertex's current distance) with
+// atomicMin; a target it improves is claimed in the level's frontier bitmap
+// slot (the same three rotating slots as the per-level kernels, so nothing
+// needs rebuilding when they take over) and, if first, appended to the
+// CTA's slice.  One cluster barrier per level; every warp reads the eight
+// slices' counters after it and takes the same decision.  The loop stops
+// after a level whose frontier is empty, holds a long row, outgrows a limit
+// or a slice (entries past it went to the global queue at once), at level
+// n - 1, or after kSmallMaxLevels levels, and that level is handed back as
+// a push level: slices -> global queue and segments, and its counters.
+__global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock)
+    sssp_small(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+               const int32_t* __restrict__ wi, const float* __restrict__ wf, int is_float, SsCtl* ctl, int32_t* q,
+               Seg* segs, size_t segcap, uint32_t* inq, int32_t n, int32_t nwords) {
+  __shared__ SmallSlice s_sl[2];
+  __shared__ int32_t s_cnt[2], s_nlong[2];
+  __shared__ uint32_t s_mf[2];
+  if (ctl->done || ctl->mode != kModeSmall) return;
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int lane = lane_id(), wib = threadIdx.x >> 5;
+  constexpr int kWarps = kSmallBlock / 32;
+  const int cwarp = rank * kWarps + wib;
+  const size_t tid = (size_t)rank * kSmallBlock + threadIdx.x;
+  const size_t stride = (size_t)kSmallCtas * kSmallBlock;
+  int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
+  const int32_t source = ctl->source;
+  const bool fl = is_float != 0;
+  if (threadIdx.x < 2) {
+    s_cnt[threadIdx.x] = 0;
+    s_nlong[threadIdx.x] = 0;
+    s_mf[threadIdx.x] = 0;
+  }
+  __syncthreads();
+
+  int L = ctl->level;
+  int pre = INT_MAX, tot = 0;  // dealing of the previous level's slices (lane r < kSmallCtas: slice r)
+  int nlev = 0;
+  unsigned long long mf = 0;
+  for (int iter = 0;; iter++) {
+    const int p = L & 1;
+    uint32_t* inq_out = inq + (size_t)(L % 3) * nwords;
+    {
+      uint32_t* clr = inq + (size_t)((L + 1) % 3) * nwords;  // claimed two levels ago; nobody reads it now
+      for (size_t i = tid; i < (size_t)nwords; i += stride) clr[i] = 0;
+    }
+    uint32_t my_mf = 0;
+    bool my_long = false;
+    auto op = [&](int k, bool valid, int32_t dv) {
+      int32_t u = valid ? __ldg(col + k) : -1;
+      bool found = false;
+      int rs = 0, deg = 0;
+      if (valid && u != source) {
+        const int32_t nd = relax_sum(dv, k, wi, wf, fl);
+        rs = __ldg(row_ptr + u);
+        const int re = __ldg(row_ptr + u + 1);
+        if (nd < atomicMin(dist + u, nd)) {
+          const uint32_t bit = 1u << (u & 31);
+          found = !(atomicOr(inq_out + (u >> 5), bit) & bit);
+        }
+        deg = re - rs;
+      }
+      if (found) {
+        my_mf += (uint32_t)deg;
+        my_long |= deg >= kLongRow;
+      }
+      const uint32_t m = __ballot_sync(kFull, found);
+      if (m == 0) return;
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&s_cnt[p], __popc(m));
+      const int slot = __shfl_sync(kFull, base, leader) + __popc(m & lanemask_lt());
+      if (found && slot < kSmallCap) {
+        s_sl[p].u[slot] = u;
+        s_sl[p].rs[slot] = rs;
+        s_sl[p].deg[slot] = deg;
+      }
+      const bool spill = found && slot >= kSmallCap;
+      if (__any_sync(kFull, spill))
+        emit_routed(spill, u, deg, rs, q + (size_t)p * n, &ctl->qsize[p], segs + (size_t)p * segcap, &ctl->lpack[p]);
+    };
+    if (iter == 0) {
+      // the previous level in the global format
+      const int pin = p ^ 1;
+      const int32_t* qin = q + (size_t)pin * n;
+      const int qn = ctl->qsize[pin], ln = seg_count(ctl->lpack[pin]);
+      const Seg* sin = segs + (size_t)pin * segcap;
+      seg_expand(row_ptr, sin, ln, [&](int32_t v, int k, bool valid) { op(k, valid, valid ? __ldcg(dist + v) : 0); });
+      const int bs = batch_rows(qn);
+      for (int b = cwarp * bs; b < qn; b += kSmallCtas * kWarps * bs) {
+        const int i = b + lane;
+        const bool ok = lane < bs && i < qn;
+        int rs = 0, deg = 0;
+        int32_t dv = 0;
+        if (ok) {
+          const int32_t v = qin[i];
+          rs = row_ptr[v];
+          deg = row_ptr[v + 1] - rs;
+          dv = __ldcg(dist + v);
+        }
+        expand_rows(ok, rs, deg, dv, op);
+      }
+    } else {
+      // the previous level's slices, across the cluster
+      const int bs = batch_rows(tot);
+      for (int b = cwarp * bs; b < tot; b += kSmallCtas * kWarps * bs) {
+        const int e = lane < bs ? b + lane : INT_MAX;
+        int r = 0;
+#pragma unroll
+        for (int step = kSmallCtas / 2; step; step >>= 1) {
+          const int ex = __shfl_sync(kFull, pre, r + step);
+          if (ex <= e) r += step;
+        }
+        const int off = e - __shfl_sync(kFull, pre, r);
+        int rs = 0, deg = 0;
+        int32_t dv = 0;
+        if (e < tot) {
+          const SmallSlice* src = cluster.map_shared_rank(&s_sl[p ^ 1], r);
+          rs = src->rs[off];
+          deg = src->deg[off];
+          dv = __ldcg(dist + src->u[off]);
+        }
+        expand_rows(e < tot, rs, deg, dv, op);
+      }
+    }
+    my_mf = __reduce_add_sync(kFull, my_mf);
+    my_long = __any_sync(kFull, my_long);
+    if (lane == 0) {
+      if (my_mf) atomicAdd(&s_mf[p], my_mf);
+      if (my_long) s_nlong[p] = 1;
+    }
+    cluster.sync();
+    int cnt = 0, nl = 0;
+    uint32_t mr = 0;
+    if (lane < kSmallCtas) {
+      cnt = *cluster.map_shared_rank(&s_cnt[p], lane);
+      nl = *cluster.map_shared_rank(&s_nlong[p], lane);
+      mr = *cluster.map_shared_rank(&s_mf[p], lane);
+    }
+    const int kept = cnt < kSmallCap ? cnt : kSmallCap;
+    int incl = kept;
+#pragma unroll
+    for (int d = 1; d < kSmallCtas; d <<= 1) {
+      const int t = __shfl_up_sync(kFull, incl, d);
+      if (lane >= d) incl += t;
+    }
+    const int nf = (int)__reduce_add_sync(kFull, (uint32_t)cnt);
+    mf = __reduce_add_sync(kFull, mr);
+    const bool longs = __any_sync(kFull, nl != 0);
+    const bool over = __any_sync(kFull, cnt > kSmallCap);
+    const bool stop = nf == 0 || longs || over || nf > kSmallFrontier || (long long)mf > kSmallEdges ||
+                      L + 1 >= n || iter + 1 == kSmallMaxLevels;
+    if (stop) break;
+    pre = lane < kSmallCtas ? incl - kept : INT_MAX;
+    tot = __shfl_sync(kFull, incl, kSmallCtas - 1);
+    nlev++;
+    if (threadIdx.x == 0) {
+      s_cnt[p ^ 1] = 0;
+      s_nlong[p ^ 1] = 0;
+      s_mf[p ^ 1] = 0;
+      if (iter == 0 && rank == 0) {
+        ctl->qsize[p ^ 1] = 0;
+        ctl->lpack[p ^ 1] = 0;
+        ctl->mf[p ^ 1] = 0;
+      }
+    }
+    if (iter == 0) cluster.sync(); else __syncthreads();
+    L++;
+  }
+
+  // hand-off of level L (slice parity p) to the per-level kernels
+  const int p = L & 1;
+  const int mine = s_cnt[p] < kSmallCap ? s_cnt[p] : kSmallCap;
+  for (int b = wib * 32; b < mine; b += kWarps * 32) {
+    const int i = b + lane;
+    const bool ok = i < mine;
+    emit_routed(ok, ok ? s_sl[p].u[i] : 0, ok ? s_sl[p].deg[i] : 0, ok ? s_sl[p].rs[i] : 0, q + (size_t)p * n,
+                &ctl->qsize[p], segs + (size_t)p * segcap, &ctl->lpack[p]);
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    ctl->mf[p] = mf;
+    ctl->n_push += nlev;
+    ctl->level = L;
+  }
+  // No CTA may exit while another still reads its counters or slices
+  // through distributed shared memory.
+  cluster.sync();
 }
 
 __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, int can_pull, cudaGraphConditionalHandle loop,
@@ -339,7 +537,7 @@ __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, int can_pull, cu
     return;
   }
   const int L = ctl->level, pout = L & 1;
-  if (ctl->mode == kModePush) ctl->n_push++; else ctl->n_pull++;
+  if (ctl->mode == kModePull) ctl->n_pull++; else ctl->n_push++;  // cluster levels are push levels
   // The reference stops after n levels at most (src/algorithm/cpu/sssp.cpp:34);
   // with non-negative weights the queue empties long before.
   if ((ctl->qsize[pout] == 0 && ctl->lpack[pout] == 0) || L >= n) {
@@ -355,6 +553,9 @@ __global__ void sssp_decide(SsCtl* __restrict__ ctl, int32_t n, int can_pull, cu
   int mode = (long long)ctl->mf[pout] * kPullRatio > ctl->m ? kModePull : kModePush;
   if (ctl->force) mode = ctl->force - 1 == kVarPull ? kModePull : kModePush;
   if (!can_pull) mode = kModePush;
+  if (mode == kModePush && ctl->small && !ctl->force && ctl->qsize[pout] <= kSmallFrontier &&
+      ctl->lpack[pout] == 0 && (long long)ctl->mf[pout] <= kSmallEdges)
+    mode = kModeSmall;
   ctl->mode = mode;
   ctl->level = L + 1;
 }
@@ -402,6 +603,7 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   SsCtl c = {};
   c.policy = DAWN_VARIANT_PUSH;
   c.force = g->force_variant == 3 ? 1 + kVarPush : g->force_variant;
+  c.small = g->small_levels && cluster_fits((const void*)sssp_small, kSmallCtas, kSmallBlock) ? 1 : 0;
   c.m = g->m;
   c.weighted = is_float;
   c.nsrc = nsrc;
@@ -459,6 +661,8 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   void* step_args[] = {&a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.ctl, &a.q, &a.segs, &a.segcap,
                        &a.inq, &a.n, &a.nwords, &a.t_row_ptr, &a.t_col, &a.t_wi, &a.t_wf, &a.ul, &a.ul_n, &a.hv,
                        &a.hv_segoff, &a.hv_count, &a.hv_segs, &a.pull_seg};
+  void* small_args[] = {&a.row_ptr, &a.col, &a.wi, &a.wf, &a.is_float, &a.ctl, &a.q, &a.segs, &a.segcap,
+                        &a.inq, &a.n, &a.nwords};
   void* decide_args[] = {&a.ctl, &a.n, &a.can_pull, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
 
@@ -467,11 +671,12 @@ dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, voi
   fam.npre = 2;
   fam.pre[0] = {(const void*)sssp_clear, clear_args, dim3(sms * 4), dim3(kBlock)};
   fam.pre[1] = {(const void*)sssp_init, init_args, dim3(1), dim3(kBlock)};
-  fam.nbody = 2;
+  fam.nbody = 3;
   fam.body[0] = {(const void*)sssp_step, step_args,
                  dim3(persistent_blocks((const void*)sssp_step, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
                  "sssp_step"};
-  fam.body[1] = {(const void*)sssp_decide, decide_args, dim3(1), dim3(32), "sssp_decide"};
+  fam.body[1] = {(const void*)sssp_small, small_args, dim3(kSmallCtas), dim3(kSmallBlock), "sssp_small", kModeSmall};
+  fam.body[2] = {(const void*)sssp_decide, decide_args, dim3(1), dim3(32), "sssp_decide"};
   fam.npost = 1;
   fam.post[0] = {(const void*)sssp_next, next_args, dim3(1), dim3(32), "sssp_next"};
   fam.ctl = a.ctl;

@@ -4,6 +4,8 @@
 // closeness reductions.
 #include <cstring>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "dawn_device.cuh"
 
@@ -60,6 +62,22 @@ void release(DevBuf& b) {
   if (b.p) pool_free(b.p, b.stream);
   b.p = nullptr;
   b.bytes = 0;
+}
+
+bool cluster_fits(const void* fn, int ctas, int threads) {
+  static std::mutex mu;
+  static std::vector<std::pair<const void*, bool>> known;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto& k : known)
+    if (k.first == fn) return k.second;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(threads);
+  int clusters = 0;
+  const bool fits = cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) == cudaSuccess && clusters > 0;
+  cudaGetLastError();
+  known.emplace_back(fn, fits);
+  return fits;
 }
 
 int persistent_blocks(const void* fn, int block, size_t smem, int cap) {

@@ -167,3 +167,34 @@ def test_batched_high_diameter_sparse_masks():
     check(g, gen.sources(g, 100, seed=77))
     k = gen.knn(3000, 6, seed=78, weights=True)
     check(k, gen.sources(k, 70, seed=79))
+
+
+def test_small_levels_change_nothing():
+    # single-source weighted traversals whose small-frontier stretches run as
+    # cluster levels, against the same calls with every level its own
+    # launch and against the oracle: a weighted grid, a weighted path longer
+    # than one cluster launch runs, a kNN graph and RMAT (hubs end the
+    # cluster levels)
+    n = 1300
+    rp = np.arange(n + 1, dtype=np.int32)
+    rp[-1] = n - 1
+    w = (np.arange(n - 1) % 7 + 1).astype(np.int32)
+    path = gen.CsrGraph(n, rp, np.arange(1, n, dtype=np.int32), w, w.astype(np.float32))
+    cases = [(gen.grid(40, 60, seed=81, weights=True), 3), (path, 0), (gen.knn(3000, 6, seed=82, weights=True), 3),
+             (gen.rmat(12, 8, seed=83, weights=True), 3)]
+    for g, ns in cases:
+        srcs = np.array([0, 1, 5], np.int32) if ns == 0 else gen.sources(g, ns, seed=84)
+        want = O.msssp(g, srcs)
+        for wt in ("i32", "f32"):
+            with abi.Graph(g, weights=wt) as dg:
+                assert dg.get_option(abi.OPT_SMALL_LEVELS) == 1
+                on, st_on = dg.sssp(srcs, variant=abi.VARIANT_DO)
+                dg.trace(True)
+                traced, _ = dg.sssp(srcs, variant=abi.VARIANT_DO)
+                dg.trace(False)
+                dg.set_option(abi.OPT_SMALL_LEVELS, 0)
+                off, st_off = dg.sssp(srcs, variant=abi.VARIANT_DO)
+            for d in (on, traced, off):
+                bad = np.argwhere(to_ref(d) != want)
+                assert bad.size == 0, (g.n, wt, bad[:5])
+            assert st_on.edges_traversed == st_off.edges_traversed
