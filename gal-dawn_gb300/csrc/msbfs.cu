@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
 
 // Push, phase 1: the active vertices' rows (short rows warp-cooperatively,
 // long rows as segments) are dealt to warps; bits new to a target are
-// atomicOr-ed into `next` unless `next` already holds them.  In list mode
+// atomicOr-ed into `next` (not visited yet at that source).  In list mode
 // the first toucher (claiming the target in a touched bitmap) queues it for
 // phase 2; in dense mode (large frontiers) no queue is kept and phase 2
 // sweeps all vertices instead.
@@ -649,8 +649,10 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
     int32_t u = -1;
     if (valid) {
       u = __ldg(col + k);
-      B bits = B::ldg(fin + (size_t)v * W).andnot(B::ldcg(visit + (size_t)u * W));
-      if (bits.any()) bits = bits.andnot(B::ldcg(nxt + (size_t)u * W));
+      // No look at `next` first: its bits are OR-ed in whether or not they
+      // are there, which saves a random load per edge (the scatter is bound
+      // by the L1/TEX traffic of its random accesses).
+      const B bits = B::ldg(fin + (size_t)v * W).andnot(B::ldcg(visit + (size_t)u * W));
       if (bits.any()) {
 #pragma unroll
         for (int i = 0; i < W; i++)
