@@ -77,6 +77,12 @@ struct BsCtl {
 };
 
 constexpr int kSlicesCleared = 4;  // slices zeroed per batch; higher ones on first use
+// Pull rows below this many in-edges are walked by one lane each; longer
+// ones are swept by the whole warp.  Packing short rows across the lanes
+// (a warp scan, a shared-memory search and a shared-memory OR per edge)
+// measured 4-10% slower: the pull is bound by its L1/TEX traffic, and the
+// lane walk adds none beyond the column loads and the gathers.
+constexpr int kPullLaneMax = 64;
 constexpr int kDeepLevel = 32;     // levels from here on are written out directly
 constexpr int kShallowBits = 5;    // level slices kept: the bits of levels below kDeepLevel
 static_assert(kDeepLevel == 1 << kShallowBits, "slices hold exactly the levels below kDeepLevel");
@@ -418,9 +424,6 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
                                                      const int32_t* __restrict__ hv_segoff, u64* __restrict__ hv_acc,
                                                      int32_t hv_count, int32_t hv_segs, int32_t pull_seg, int32_t n) {
   using B = Bits<W>;
-  __shared__ int s_excl[kBlock / 32][32];
-  __shared__ int s_rs[kBlock / 32][32];
-  __shared__ u64 s_acc[kBlock / 32][32][W];
   __shared__ int32_t s_qa[kBlock / 32][kWarpQueue];
   __shared__ int32_t s_qu[kBlock / 32][kWarpQueue];
   if (ctl->done || ctl->mode != kModePull) return;
@@ -534,7 +537,7 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
     }
     const int deg = re - rs;
     B got = B::zero();
-    uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
+    uint32_t big = __ballot_sync(kFull, deg >= kPullLaneMax);
     while (big) {
       const int leader = __ffs(big) - 1;
       big &= big - 1;
@@ -556,41 +559,25 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
       w = w.warp_or();
       if (lane == leader) got = w;
     }
-    const int sdeg = deg < kWarpRow ? deg : 0;
-    const int incl = warp_incl_scan(sdeg);
-    const int total = __shfl_sync(kFull, incl, 31);
-    s_excl[wib][lane] = incl - sdeg;
-    s_rs[wib][lane] = rs;
-#pragma unroll
-    for (int i = 0; i < W; i++) s_acc[wib][lane][i] = 0ull;
-    __syncwarp();
-    // Two edges per lane per pass: both searches and both gathers are
-    // independent, so their latencies overlap.
-    for (int e0 = 0; e0 < total; e0 += 64) {
-      const int ea = e0 + lane, eb = ea + 32;
-      int lo = 0, hi = 31, lo2 = 0, hi2 = 31;
-#pragma unroll
-      for (int it = 0; it < 5; it++) {
-        const int mid = (lo + hi + 1) >> 1, mid2 = (lo2 + hi2 + 1) >> 1;
-        if (s_excl[wib][mid] <= ea) lo = mid; else hi = mid - 1;
-        if (s_excl[wib][mid2] <= eb) lo2 = mid2; else hi2 = mid2 - 1;
+    // Short rows: each lane walks its own row, four in-neighbours in
+    // flight, and stops once its missing bits are all found.  No shared
+    // memory and no search per edge: the L1/TEX path carries only the
+    // column loads and the gathers.
+    if (active && deg < kPullLaneMax) {
+      B w = B::zero();
+      for (int k = rs; k < re; k += 4) {
+        const int32_t c0 = __ldg(t_col + k);
+        const int32_t c1 = k + 1 < re ? __ldg(t_col + k + 1) : -1;
+        const int32_t c2 = k + 2 < re ? __ldg(t_col + k + 2) : -1;
+        const int32_t c3 = k + 3 < re ? __ldg(t_col + k + 3) : -1;
+        w = w | B::ldg(fin + (size_t)c0 * W);
+        if (c1 >= 0) w = w | B::ldg(fin + (size_t)c1 * W);
+        if (c2 >= 0) w = w | B::ldg(fin + (size_t)c2 * W);
+        if (c3 >= 0) w = w | B::ldg(fin + (size_t)c3 * W);
+        if ((w | vis) == full) break;
       }
-      const int32_t va = ea < total ? __ldg(t_col + s_rs[wib][lo] + (ea - s_excl[wib][lo])) : -1;
-      const int32_t vb = eb < total ? __ldg(t_col + s_rs[wib][lo2] + (eb - s_excl[wib][lo2])) : -1;
-      const B xa = va >= 0 ? B::ldg(fin + (size_t)va * W) : B::zero();
-      const B xb = vb >= 0 ? B::ldg(fin + (size_t)vb * W) : B::zero();
-#pragma unroll
-      for (int i = 0; i < W; i++) {
-        if (xa.w[i]) atomicOr(&s_acc[wib][lo][i], xa.w[i]);
-        if (xb.w[i]) atomicOr(&s_acc[wib][lo2][i], xb.w[i]);
-      }
+      got = w;
     }
-    __syncwarp();
-    if (sdeg > 0) {
-#pragma unroll
-      for (int i = 0; i < W; i++) got.w[i] = s_acc[wib][lane][i];
-    }
-    __syncwarp();
     const B nw = active ? got.andnot(vis) : B::zero();
     const bool has = nw.any();
     const bool still = active && !((vis | nw) == full);
