@@ -42,6 +42,7 @@ namespace {
 using u64 = unsigned long long;
 constexpr int kPartBlock = 1024;
 constexpr int kPartSlices = 8;  // level slices kept in registers by the emit pass
+constexpr int kPartLaneMax = 64;  // rows below this many entries are walked by one lane
 
 struct PartsCtl {
   int32_t next_task;    // task counter of the persistent grid
@@ -71,20 +72,6 @@ __device__ __forceinline__ unsigned sm_id() {
 __device__ __forceinline__ u64 block_reduce_add(u64 x, u64* s_slot) {
   x = warp_sum(x);
   if (lane_id() == 0 && x) atomicAdd(s_slot, x);
-  return x;
-}
-
-// Inclusive OR-scan of x over runs of lanes with equal key (keys must not
-// decrease from lane to lane): the last lane of a run ends with the OR of
-// the run.
-__device__ __forceinline__ u64 seg_or_scan(u64 x, int key) {
-  const int lane = lane_id();
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    const u64 y = __shfl_up_sync(kFull, x, d);
-    const int ky = __shfl_up_sync(kFull, key, d);
-    if (lane >= d && ky == key) x |= y;
-  }
   return x;
 }
 
@@ -123,9 +110,6 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
                                                            int32_t maxn) {
   __shared__ int s_task;
   __shared__ u64 s_mf, s_dec, s_nf;
-  __shared__ int s_excl[kPartBlock / 32][32];
-  __shared__ int s_rs[kPartBlock / 32][32];
-  __shared__ u64 s_w[kPartBlock / 32][32];
   const int tid = threadIdx.x;
   const int lane = lane_id(), wib = tid >> 5;
   u64* const visit = scratch + (size_t)blockIdx.x * slot_words;
@@ -191,9 +175,9 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
       }
       if (push) {
         // scatter: the frontier rows of 32 consecutive vertices per warp
-        // task; rows of >= kWarpRow entries swept by the whole warp, shorter
-        // ones concatenated across the lanes (coalesced col loads, 32
-        // independent visited loads in flight)
+        // task; rows of >= kPartLaneMax entries swept by the whole warp,
+        // shorter ones walked by one lane each (no shared-memory search per
+        // edge: these loops are bound by their L1/TEX traffic)
         for (int base = wib * 32; base < np; base += kPartBlock) {
           const int v = base + lane;
           const u64 f = v < np ? cur[v] : 0ull;
@@ -204,7 +188,7 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
           }
           const int deg = re - rs;
           if (__ballot_sync(kFull, deg > 0) == 0u) continue;
-          uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
+          uint32_t big = __ballot_sync(kFull, deg >= kPartLaneMax);
           while (big) {
             const int leader = __ffs(big) - 1;
             big &= big - 1;
@@ -216,25 +200,20 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
               if (bits) atomicOr(acc + u, bits);
             }
           }
-          const int sdeg = deg < kWarpRow ? deg : 0;
-          const int incl = warp_incl_scan(sdeg);
-          const int total = __shfl_sync(kFull, incl, 31);
-          s_excl[wib][lane] = incl - sdeg;
-          s_rs[wib][lane] = rs;
-          s_w[wib][lane] = f;
-          __syncwarp();
-          for (int e = lane; e < total; e += 32) {
-            int lo = 0, hi = 31;
+          // short rows: one lane each, four targets in flight
+          if (deg > 0 && deg < kPartLaneMax) {
+            for (int k = rs; k < re; k += 4) {
+              int u[4];
 #pragma unroll
-            for (int it = 0; it < 5; it++) {
-              const int mid = (lo + hi + 1) >> 1;
-              if (s_excl[wib][mid] <= e) lo = mid; else hi = mid - 1;
+              for (int j = 0; j < 4; j++) u[j] = k + j < re ? __ldg(col + k + j) - v0 : -1;
+              u64 bits[4];
+#pragma unroll
+              for (int j = 0; j < 4; j++) bits[j] = u[j] >= 0 ? f & ~visit[u[j]] : 0ull;
+#pragma unroll
+              for (int j = 0; j < 4; j++)
+                if (bits[j]) atomicOr(acc + u[j], bits[j]);
             }
-            const int u = __ldg(col + s_rs[wib][lo] + (e - s_excl[wib][lo])) - v0;
-            const u64 bits = s_w[wib][lo] & ~visit[u];
-            if (bits) atomicOr(acc + u, bits);
           }
-          __syncwarp();
         }
       }
       __syncthreads();
@@ -254,8 +233,8 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
           }
         } else {
           // pull: unfinished vertices OR their in-neighbours' frontier
-          // words; long rows by the whole warp with early exit, short rows
-          // concatenated and OR-ed into per-lane shared slots
+          // words; long rows by the whole warp, short rows by one lane
+          // each, both stopping once no missing bit is left
           const bool active = vis != full;
           int rs = 0, re = 0;
           if (active) {
@@ -264,7 +243,7 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
           }
           const int deg = re - rs;
           u64 got = 0ull;
-          uint32_t big = __ballot_sync(kFull, deg >= kWarpRow);
+          uint32_t big = __ballot_sync(kFull, deg >= kPartLaneMax);
           while (big) {
             const int leader = __ffs(big) - 1;
             big &= big - 1;
@@ -286,41 +265,21 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
             w = warp_or(w);
             if (lane == leader) got = w;
           }
-          const int sdeg = deg < kWarpRow ? deg : 0;
-          const int incl = warp_incl_scan(sdeg);
-          const int total = __shfl_sync(kFull, incl, 31);
-          s_excl[wib][lane] = incl - sdeg;
-          s_rs[wib][lane] = rs;
-          s_w[wib][lane] = 0ull;
-          __syncwarp();
-          for (int e0 = 0; e0 < total; e0 += 64) {
-            const int ea = e0 + lane, eb = ea + 32;
-            int lo = 0, hi = 31, lo2 = 0, hi2 = 31;
+          // short rows: one lane each, four in-neighbours in flight,
+          // stopping once the missing bits are all found
+          if (active && deg < kPartLaneMax) {
+            u64 w = 0ull;
+            for (int k = rs; k < re; k += 4) {
+              int32_t c[4];
 #pragma unroll
-            for (int it = 0; it < 5; it++) {
-              const int mid = (lo + hi + 1) >> 1, mid2 = (lo2 + hi2 + 1) >> 1;
-              if (s_excl[wib][mid] <= ea) lo = mid; else hi = mid - 1;
-              if (s_excl[wib][mid2] <= eb) lo2 = mid2; else hi2 = mid2 - 1;
+              for (int j = 0; j < 4; j++) c[j] = k + j < re ? __ldg(t_col + k + j) : -1;
+#pragma unroll
+              for (int j = 0; j < 4; j++)
+                if (c[j] >= 0) w |= cur[c[j] - v0];
+              if ((w | vis) == full) break;
             }
-            const int32_t ca = ea < total ? __ldg(t_col + s_rs[wib][lo] + (ea - s_excl[wib][lo])) : -1;
-            const int32_t cb = eb < total ? __ldg(t_col + s_rs[wib][lo2] + (eb - s_excl[wib][lo2])) : -1;
-            u64 xa = ca >= 0 ? cur[ca - v0] : 0ull;
-            u64 xb = cb >= 0 ? cur[cb - v0] : 0ull;
-            // Lanes holding edges of one row are adjacent: OR them with a
-            // segmented warp scan, then the last lane of each row adds the
-            // row's bits to its slot (no two lanes write one slot at once).
-            const int ka = ea < total ? lo : 32, kb = eb < total ? lo2 : 32;
-            xa = seg_or_scan(xa, ka);
-            xb = seg_or_scan(xb, kb);
-            const int na = __shfl_down_sync(kFull, ka, 1), nb2 = __shfl_down_sync(kFull, kb, 1);
-            if (ka < 32 && (lane == 31 || na != ka) && xa) s_w[wib][ka] |= xa;
-            __syncwarp();
-            if (kb < 32 && (lane == 31 || nb2 != kb) && xb) s_w[wib][kb] |= xb;
-            __syncwarp();
+            got = w;
           }
-          __syncwarp();
-          if (sdeg > 0) got = s_w[wib][lane];
-          __syncwarp();
           nw = got & ~vis;
         }
         if (!in) continue;
