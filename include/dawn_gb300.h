@@ -266,13 +266,15 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources,
  *                          carve-out shrinks the L2 the gathers also use), even
  *                          at scales 21 and 24. */
 #define DAWN_OPT_L2_PERSIST 8
-/*   DAWN_OPT_SMALL_LEVELS  1 (default): single-source direction-optimising
- *                          BFS runs stretches of levels whose frontier holds
- *                          at most 8192 vertices and 131072 out-edges inside
- *                          one launch of a thread-block cluster (8 CTAs,
- *                          cluster barriers between levels), instead of two
- *                          launches per level.  0: every level is its own
- *                          push or pull launch.  Distances are the same. */
+/*   DAWN_OPT_SMALL_LEVELS  1 (default): single-source traversals (BFS with
+ *                          DAWN_VARIANT_DO, weighted distances with
+ *                          DAWN_VARIANT_DO / PUSH) run stretches of levels
+ *                          whose frontier holds at most 8192 vertices and
+ *                          32768 out-edges, and no row of 128 entries or
+ *                          more, inside one launch of a thread-block cluster
+ *                          (8 CTAs, one cluster barrier per level), instead
+ *                          of two launches per level.  0: every level is its
+ *                          own launch.  Distances are the same. */
 #define DAWN_OPT_SMALL_LEVELS 9
 
 /* Autotuner (no counterpart in the reference, whose launch shapes are fixed
