@@ -564,16 +564,19 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
     // memory and no search per edge: the L1/TEX path carries only the
     // column loads and the gathers.
     if (active && deg < kPullLaneMax) {
+      // The row is read in 32-byte aligned chunks of eight entries, two
+      // 16-byte loads each (the first from before the row start when it is
+      // not aligned; in-edge arrays carry 16 spare bytes, so neither load
+      // passes their end), so a lane issues two column loads per eight
+      // gathers instead of eight.
       B w = B::zero();
-      for (int k = rs; k < re; k += 4) {
-        const int32_t c0 = __ldg(t_col + k);
-        const int32_t c1 = k + 1 < re ? __ldg(t_col + k + 1) : -1;
-        const int32_t c2 = k + 2 < re ? __ldg(t_col + k + 2) : -1;
-        const int32_t c3 = k + 3 < re ? __ldg(t_col + k + 3) : -1;
-        w = w | B::ldg(fin + (size_t)c0 * W);
-        if (c1 >= 0) w = w | B::ldg(fin + (size_t)c1 * W);
-        if (c2 >= 0) w = w | B::ldg(fin + (size_t)c2 * W);
-        if (c3 >= 0) w = w | B::ldg(fin + (size_t)c3 * W);
+      for (int a = rs & ~7; a < re; a += 8) {
+        const int4 x = __ldg(reinterpret_cast<const int4*>(t_col + a));
+        const int4 y = a + 4 < re ? __ldg(reinterpret_cast<const int4*>(t_col + a + 4)) : make_int4(0, 0, 0, 0);
+        const int32_t c[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          if (a + j >= rs && a + j < re) w = w | B::ldg(fin + (size_t)c[j] * W);
         if ((w | vis) == full) break;
       }
       got = w;
