@@ -287,7 +287,9 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
         nxt[u] = nw;
         if (nw) {
           visit[u] = vis | nw;
-          for (unsigned l = (unsigned)L; l; l &= l - 1) slices[(size_t)(__ffs(l) - 1) * maxn + u] |= nw;
+          // the bits are new to every slice, so an OR without a return
+          // (no load on the thread's path) records them
+          for (unsigned l = (unsigned)L; l; l &= l - 1) atomicOr(slices + (size_t)(__ffs(l) - 1) * maxn + u, nw);
           const int gu = v0 + u;
           const u64 od = (u64)(row_ptr[gu + 1] - row_ptr[gu]);
           lmf += od;
