@@ -222,26 +222,31 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
       for (int base = wib * 32; base < np; base += kPartBlock) {
         const int u = base + lane;
         const bool in = u < np;
-        const u64 vis = in ? visit[u] : full;
+        const int gu = v0 + u;
+        // every load of the vertex's own words and row bounds is issued at
+        // once, ahead of the gathers that need them
+        u64 vis = full, x = 0ull;
+        int rp0 = 0, rp1 = 0, tr0 = 0, tr1 = 0;
+        if (in) {
+          vis = visit[u];
+          rp0 = row_ptr[gu];
+          rp1 = row_ptr[gu + 1];
+          tr0 = t_row_ptr[gu];
+          tr1 = t_row_ptr[gu + 1];
+          if (push) x = acc[u];
+        }
         u64 nw = 0ull;
         if (push) {
-          if (in) {
-            const u64 x = acc[u];
-            if (x) {
-              acc[u] = 0ull;
-              nw = x & ~vis;
-            }
+          if (x) {
+            acc[u] = 0ull;
+            nw = x & ~vis;
           }
         } else {
           // pull: unfinished vertices OR their in-neighbours' frontier
           // words; long rows by the whole warp, short rows by one lane
           // each, both stopping once no missing bit is left
           const bool active = vis != full;
-          int rs = 0, re = 0;
-          if (active) {
-            rs = t_row_ptr[v0 + u];
-            re = t_row_ptr[v0 + u + 1];
-          }
+          const int rs = active ? tr0 : 0, re = active ? tr1 : 0;
           const int deg = re - rs;
           u64 got = 0ull;
           uint32_t big = __ballot_sync(kFull, deg >= kPartLaneMax);
@@ -290,12 +295,11 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
           // the bits are new to every slice, so an OR without a return
           // (no load on the thread's path) records them
           for (unsigned l = (unsigned)L; l; l &= l - 1) atomicOr(slices + (size_t)(__ffs(l) - 1) * maxn + u, nw);
-          const int gu = v0 + u;
-          const u64 od = (u64)(row_ptr[gu + 1] - row_ptr[gu]);
+          const u64 od = (u64)(rp1 - rp0);
           lmf += od;
           my_reached += od * (u64)__popcll(nw);
           lnf++;
-          if ((vis | nw) == full) ldec += (u64)(t_row_ptr[gu + 1] - t_row_ptr[gu]);
+          if ((vis | nw) == full) ldec += (u64)(tr1 - tr0);
         }
       }
       block_reduce_add(lmf, &s_mf);
