@@ -8,15 +8,17 @@
 // range [off[p], off[p+1]) and no edge leaves its part), and one persistent
 // kernel runs every (part, batch of up to 64 sources) task:
 //
-//   * a CTA takes the next task from a device counter (tasks sorted by part
-//     size, largest first, so the long ones start early) and runs the whole
-//     multi-source bitset traversal of that part on its own, with
-//     __syncthreads between phases: no launch per level, no host sync, and
-//     no wait on another CTA;
-//   * its working words live in a per-CTA slot of global memory (visited,
-//     two frontier words, a push accumulator and bit-sliced levels, one
-//     uint64 per vertex each); the part's words stay in L2 while the CTA
-//     works on them;
+//   * a thread-block cluster (kPartCluster CTAs on as many SMs) takes the
+//     next task from a device counter (tasks sorted by estimated cost,
+//     longest first, so the long ones start early) and runs the whole
+//     multi-source bitset traversal of that part, its CTAs splitting every
+//     vertex and row sweep, with cluster barriers between phases and the
+//     level counters summed through distributed shared memory: no launch
+//     per level, no host sync, and no wait on another cluster;
+//   * its working words live in a per-cluster slot of global memory
+//     (visited, two frontier words, a push accumulator and bit-sliced
+//     levels, one uint64 per vertex each); the part's words stay in L2
+//     while the cluster works on them;
 //   * each level is a push (frontier rows scattered with atomicOr into the
 //     accumulator, then a sweep folding it in) or a pull (each unfinished
 //     vertex ORs its in-neighbours' frontier words, stopping once no
@@ -30,6 +32,8 @@
 // Hop distances are those of a separate BFS of each part from each source:
 // bit b of a vertex's word appears at level L exactly when source b first
 // reaches it at L, whatever the direction of each level.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -44,6 +48,7 @@ using u64 = unsigned long long;
 constexpr int kPartBlock = 1024;
 constexpr int kPartSlices = 8;  // level slices kept in registers by the emit pass
 constexpr int kPartLaneMax = 64;  // rows below this many entries are walked by one lane
+constexpr int kPartCluster = 8;   // CTAs (SMs) per task: a thread-block cluster
 
 struct PartsCtl {
   int32_t next_task;    // task counter of the persistent grid
@@ -101,7 +106,8 @@ __device__ __forceinline__ void emit_part_vertex(int32_t* __restrict__ dist, int
   for (int k = NB; k < nbits; k++) slices[(size_t)k * maxn + u] = 0ull;
 }
 
-__global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __restrict__ ctl,
+__global__ void __cluster_dims__(kPartCluster, 1, 1) __launch_bounds__(kPartBlock, 1)
+    parts_traverse(PartsCtl* __restrict__ ctl,
                                                            const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ col,
                                                            const int32_t* __restrict__ t_row_ptr,
@@ -109,11 +115,22 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
                                                            const int32_t* __restrict__ voff,
                                                            u64* __restrict__ scratch, size_t slot_words,
                                                            int32_t maxn) {
+  // Per level (by parity): frontier out-edges, in-edges of the vertices
+  // finished, vertices reached.  Each CTA counts its own; the cluster's
+  // totals are read through distributed shared memory after the level's
+  // barrier, and a CTA resets its counters of the other parity then (every
+  // reader of those passed the barrier).
   __shared__ int s_task;
-  __shared__ u64 s_mf, s_dec, s_nf;
+  __shared__ u64 s_cnt[2][3];
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int crank = (int)cluster.block_rank();
   const int tid = threadIdx.x;
+  const int ctid = crank * kPartBlock + tid;  // thread index within the cluster
+  constexpr int kThreads = kPartCluster * kPartBlock;
   const int lane = lane_id(), wib = tid >> 5;
-  u64* const visit = scratch + (size_t)blockIdx.x * slot_words;
+  const int cwarp = crank * (kPartBlock / 32) + wib;
+  u64* const visit = scratch + (size_t)(blockIdx.x / kPartCluster) * slot_words;
   u64* const fa = visit + maxn;
   u64* const fb = fa + maxn;
   u64* const acc = fb + maxn;
@@ -122,10 +139,21 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
   u64 my_reached = 0;
   u64 t_levels = 0, t_push = 0, t_pull = 0;
 
+  auto totals = [&](int par, u64& mf_t, u64& dec_t, u64& nf_t) {
+    mf_t = dec_t = nf_t = 0;
+#pragma unroll
+    for (int r = 0; r < kPartCluster; r++) {
+      const u64* c = cluster.map_shared_rank(&s_cnt[par][0], r);
+      mf_t += c[0];
+      dec_t += c[1];
+      nf_t += c[2];
+    }
+  };
   for (;;) {
-    if (tid == 0) s_task = atomicAdd(&ctl->next_task, 1);
-    __syncthreads();
-    const int t = s_task;
+    if (crank == 0 && tid == 0) s_task = atomicAdd(&ctl->next_task, 1);
+    if (tid < 6) (&s_cnt[0][0])[tid] = 0;
+    cluster.sync();
+    const int t = *cluster.map_shared_rank(&s_task, 0);
     if (t >= ctl->ntasks) break;
     const PartTask task = ctl->tasks[t];
     const int32_t v0 = voff[task.part];
@@ -135,51 +163,46 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
     const int32_t* src = ctl->sources + task.src0;
     const long long mp = (long long)row_ptr[v0 + np] - row_ptr[v0];
     unsigned long long t_start = 0, push0 = t_push;
-    if (tid == 0 && ctl->task_log) t_start = global_ns();
-    if (tid == 0) {
-      s_mf = 0;
-      s_dec = 0;
-      s_nf = 0;
+    if (ctid == 0 && ctl->task_log) t_start = global_ns();
+    // Seed: source b sets bit b at its vertex (the cluster's first CTA;
+    // its level-0 counters take the seeds' rows).
+    if (ctid < nb) {
+      const int32_t s = src[ctid];
+      atomicOr(visit + s, 1ull << ctid);
+      atomicOr(fa + s, 1ull << ctid);
     }
     __syncthreads();
-    // Seed: source b sets bit b at its vertex.
-    if (tid < nb) {
-      const int32_t s = src[tid];
-      atomicOr(visit + s, 1ull << tid);
-      atomicOr(fa + s, 1ull << tid);
-    }
-    __syncthreads();
-    if (tid < nb) {
-      const int32_t s = src[tid];
+    if (ctid < nb) {
+      const int32_t s = src[ctid];
       const int32_t gs = v0 + s;
       const u64 deg = (u64)(row_ptr[gs + 1] - row_ptr[gs]);
       my_reached += deg;
       // the thread of the lowest bit at a vertex counts the vertex once
-      if ((fa[s] & ((1ull << tid) - 1ull)) == 0ull) {
-        atomicAdd(&s_mf, deg);
-        if (visit[s] == full) atomicAdd(&s_dec, (u64)(t_row_ptr[gs + 1] - t_row_ptr[gs]));
+      if ((fa[s] & ((1ull << ctid) - 1ull)) == 0ull) {
+        atomicAdd(&s_cnt[0][0], deg);
+        if (visit[s] == full) atomicAdd(&s_cnt[0][1], (u64)(t_row_ptr[gs + 1] - t_row_ptr[gs]));
       }
     }
-    __syncthreads();
-    long long mf = (long long)s_mf;
-    long long mu = mp - (long long)s_dec;
+    cluster.sync();
+    long long mf, mu;
+    {
+      u64 a0, a1, a2;
+      totals(0, a0, a1, a2);
+      mf = (long long)a0;
+      mu = mp - (long long)a1;
+    }
     u64* cur = fa;
     u64* nxt = fb;
     int L = 1;
     for (;;) {
       const bool push = mf * ratio < mu;
-      __syncthreads();  // every thread has read the counters of the last level
-      if (tid == 0) {
-        s_mf = 0;
-        s_dec = 0;
-        s_nf = 0;
-      }
+      const int par = L & 1;  // this level's counters; level 0 used the other parity
       if (push) {
         // scatter: the frontier rows of 32 consecutive vertices per warp
         // task; rows of >= kPartLaneMax entries swept by the whole warp,
         // shorter ones walked by one lane each (no shared-memory search per
         // edge: these loops are bound by their L1/TEX traffic)
-        for (int base = wib * 32; base < np; base += kPartBlock) {
+        for (int base = cwarp * 32; base < np; base += kThreads) {
           const int v = base + lane;
           const u64 f = v < np ? cur[v] : 0ull;
           int rs = 0, re = 0;
@@ -217,9 +240,9 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
           }
         }
       }
-      __syncthreads();
+      if (push) cluster.sync();  // the scatter's ORs are in before the sweep reads them
       u64 lmf = 0, ldec = 0, lnf = 0;
-      for (int base = wib * 32; base < np; base += kPartBlock) {
+      for (int base = cwarp * 32; base < np; base += kThreads) {
         const int u = base + lane;
         const bool in = u < np;
         const int gu = v0 + u;
@@ -302,14 +325,20 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
           if ((vis | nw) == full) ldec += (u64)(tr1 - tr0);
         }
       }
-      block_reduce_add(lmf, &s_mf);
-      block_reduce_add(ldec, &s_dec);
-      block_reduce_add(lnf, &s_nf);
+      block_reduce_add(lmf, &s_cnt[par][0]);
+      block_reduce_add(ldec, &s_cnt[par][1]);
+      block_reduce_add(lnf, &s_cnt[par][2]);
       if (push) t_push++; else t_pull++;
+      cluster.sync();
+      u64 mf_t, dec_t, nf_t;
+      totals(par, mf_t, dec_t, nf_t);
+      // every reader of the other parity's counters is past the barrier,
+      // and this CTA's next-level sums wait for the reset
+      if (tid < 3) s_cnt[par ^ 1][tid] = 0;
       __syncthreads();
-      if (s_nf == 0 || L >= np) break;
-      mf = (long long)s_mf;
-      mu -= (long long)s_dec;
+      if (nf_t == 0 || L >= np) break;
+      mf = (long long)mf_t;
+      mu -= (long long)dec_t;
       u64* tmp = cur;
       cur = nxt;
       nxt = tmp;
@@ -320,7 +349,7 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
     const int deepest = L - 1;
     const int nbits = deepest > 0 ? 32 - __clz(deepest) : 0;
     int32_t* dist = ctl->dist + task.out0;
-    for (int u = tid; u < np; u += kPartBlock) {
+    for (int u = ctid; u < np; u += kThreads) {
       const u64 vis = visit[u];
       visit[u] = 0ull;
       fa[u] = 0ull;
@@ -337,8 +366,8 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
         default: emit_part_vertex<kPartSlices>(dist, np, nb, u, vis, slices, maxn, nbits); break;
       }
     }
-    __syncthreads();  // the slot is clean before the next task seeds it
-    if (tid == 0 && ctl->task_log) {
+    cluster.sync();  // the slot is clean before the next task seeds it
+    if (ctid == 0 && ctl->task_log) {
       unsigned long long* r = ctl->task_log + 4 * (size_t)t;
       r[0] = t_start;
       r[1] = global_ns();
@@ -346,9 +375,10 @@ __global__ void __launch_bounds__(kPartBlock, 1) parts_traverse(PartsCtl* __rest
       r[3] = sm_id();
     }
   }
+  cluster.sync();  // no CTA exits while another may still read its task slot
   my_reached = warp_sum(my_reached);
   if (lane_id() == 0 && my_reached) atomicAdd(&ctl->reached, my_reached);
-  if (tid == 0 && t_levels) {
+  if (ctid == 0 && t_levels) {
     atomicAdd(&ctl->levels, t_levels);
     atomicAdd(&ctl->push_levels, t_push);
     atomicAdd(&ctl->pull_levels, t_pull);
@@ -476,14 +506,24 @@ dawn_status parts_set(dawn_graph* g, int32_t nparts, const int32_t* offsets) {
       return DAWN_ERR_INVALID_ARG;
     }
   }
-  // Per-CTA slots: visited, two frontiers, accumulator and one slice per
-  // level bit (levels never exceed the part's vertex count).
+  // Per-cluster slots: visited, two frontiers, accumulator and one slice
+  // per level bit (levels never exceed the part's vertex count).  The grid
+  // is as many clusters as the device holds at once.
   const int nbits = 32 - __builtin_clz((unsigned)maxn);
   const size_t slot_words = (size_t)(4 + nbits) * (size_t)maxn;
-  int per_sm = 0;
-  DAWN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, parts_traverse, kPartBlock, 0));
-  const int slots = g->geo.sms * std::max(per_sm, 1);
-  const size_t bytes = sizeof(u64) * slot_words * (size_t)slots;
+  int clusters = 0;
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kPartCluster);
+    cfg.blockDim = dim3(kPartBlock);
+    if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)parts_traverse, &cfg) != cudaSuccess ||
+        clusters < 1) {
+      cudaGetLastError();
+      clusters = std::max(1, g->geo.sms / kPartCluster);
+    }
+  }
+  const int slots = clusters * kPartCluster;  // CTAs of the grid
+  const size_t bytes = sizeof(u64) * slot_words * (size_t)clusters;
   if (g->pt_scratch.bytes < bytes) {
     DAWN_CHECK(ensure(g->pt_scratch, bytes, g->stream));
     if (g->pt_exec) {
