@@ -644,10 +644,16 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
       // by the L1/TEX traffic of its random accesses).
       const B bits = B::ldg(fin + (size_t)v * W).andnot(B::ldcg(visit + (size_t)u * W));
       if (bits.any()) {
+        if (W == 1 && !dense) {
+          // one word: the OR that finds it empty is the first touch (no
+          // touched bitmap to claim in and clear again)
+          first = atomicOr(nxt + u, bits.w[0]) == 0ull;
+        } else {
 #pragma unroll
-        for (int i = 0; i < W; i++)
-          if (bits.w[i]) atomicOr(nxt + (size_t)u * W + i, bits.w[i]);
-        if (!dense) first = claim_bit(tbm, u);
+          for (int i = 0; i < W; i++)
+            if (bits.w[i]) atomicOr(nxt + (size_t)u * W + i, bits.w[i]);
+          if (!dense) first = claim_bit(tbm, u);
+        }
       }
     }
     if (!dense) wq.push(first, u);
@@ -690,7 +696,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
     int odeg = 0, ors = 0;
     if (i < tn) {
       u = dense ? i : tq[i];
-      if (!dense) atomicAnd(tbm + (u >> 5), ~(1u << (u & 31)));
+      if (!dense && W > 1) atomicAnd(tbm + (u >> 5), ~(1u << (u & 31)));
       const B x = B::ld(nxt + (size_t)u * W);
       if (x.any()) {
         B::zero().st(nxt + (size_t)u * W);
