@@ -236,6 +236,7 @@ struct dawn_graph {
   dawn::DevBuf pt_voff, pt_tasks, pt_sources, pt_ctl, pt_scratch, pt_rows;
   size_t pt_slot_words = 0;
   int32_t pt_slots = 0, pt_maxn = 0;
+  int32_t pt_cluster = 1;  // CTAs per task of the multi-graph launch
   cudaGraphExec_t pt_exec = nullptr;
 
   // closeness reduction

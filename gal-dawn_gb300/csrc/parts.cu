@@ -48,7 +48,7 @@ using u64 = unsigned long long;
 constexpr int kPartBlock = 1024;
 constexpr int kPartSlices = 8;  // level slices kept in registers by the emit pass
 constexpr int kPartLaneMax = 64;  // rows below this many entries are walked by one lane
-constexpr int kPartCluster = 8;   // CTAs (SMs) per task: a thread-block cluster
+constexpr int kPartCluster = 8;   // CTAs (SMs) per task: a thread-block cluster (1 where 8 do not fit)
 
 struct PartsCtl {
   int32_t next_task;    // task counter of the persistent grid
@@ -106,7 +106,8 @@ __device__ __forceinline__ void emit_part_vertex(int32_t* __restrict__ dist, int
   for (int k = NB; k < nbits; k++) slices[(size_t)k * maxn + u] = 0ull;
 }
 
-__global__ void __cluster_dims__(kPartCluster, 1, 1) __launch_bounds__(kPartBlock, 1)
+template <int C>
+__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(kPartBlock, 1)
     parts_traverse(PartsCtl* __restrict__ ctl,
                                                            const int32_t* __restrict__ row_ptr,
                                                            const int32_t* __restrict__ col,
@@ -127,10 +128,10 @@ __global__ void __cluster_dims__(kPartCluster, 1, 1) __launch_bounds__(kPartBloc
   const int crank = (int)cluster.block_rank();
   const int tid = threadIdx.x;
   const int ctid = crank * kPartBlock + tid;  // thread index within the cluster
-  constexpr int kThreads = kPartCluster * kPartBlock;
+  constexpr int kThreads = C * kPartBlock;
   const int lane = lane_id(), wib = tid >> 5;
   const int cwarp = crank * (kPartBlock / 32) + wib;
-  u64* const visit = scratch + (size_t)(blockIdx.x / kPartCluster) * slot_words;
+  u64* const visit = scratch + (size_t)(blockIdx.x / C) * slot_words;
   u64* const fa = visit + maxn;
   u64* const fb = fa + maxn;
   u64* const acc = fb + maxn;
@@ -142,7 +143,7 @@ __global__ void __cluster_dims__(kPartCluster, 1, 1) __launch_bounds__(kPartBloc
   auto totals = [&](int par, u64& mf_t, u64& dec_t, u64& nf_t) {
     mf_t = dec_t = nf_t = 0;
 #pragma unroll
-    for (int r = 0; r < kPartCluster; r++) {
+    for (int r = 0; r < C; r++) {
       const u64* c = cluster.map_shared_rank(&s_cnt[par][0], r);
       mf_t += c[0];
       dec_t += c[1];
@@ -511,18 +512,21 @@ dawn_status parts_set(dawn_graph* g, int32_t nparts, const int32_t* offsets) {
   // is as many clusters as the device holds at once.
   const int nbits = 32 - __builtin_clz((unsigned)maxn);
   const size_t slot_words = (size_t)(4 + nbits) * (size_t)maxn;
-  int clusters = 0;
+  int cluster = kPartCluster, clusters = 0;
   {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(kPartCluster);
     cfg.blockDim = dim3(kPartBlock);
-    if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)parts_traverse, &cfg) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveClusters(&clusters, (const void*)parts_traverse<kPartCluster>, &cfg) != cudaSuccess ||
         clusters < 1) {
+      // no room for clusters of kPartCluster CTAs (a small partition of the
+      // device): one CTA per task, one per SM
       cudaGetLastError();
-      clusters = std::max(1, g->geo.sms / kPartCluster);
+      cluster = 1;
+      clusters = g->geo.sms;
     }
   }
-  const int slots = clusters * kPartCluster;  // CTAs of the grid
+  const int slots = clusters * cluster;  // CTAs of the grid
   const size_t bytes = sizeof(u64) * slot_words * (size_t)clusters;
   if (g->pt_scratch.bytes < bytes) {
     DAWN_CHECK(ensure(g->pt_scratch, bytes, g->stream));
@@ -533,12 +537,14 @@ dawn_status parts_set(dawn_graph* g, int32_t nparts, const int32_t* offsets) {
   }
   // Slots are clean between calls: each task zeroes what it used.
   DAWN_CUDA(cudaMemsetAsync(g->pt_scratch.p, 0, bytes, g->stream));
-  if (g->pt_exec && (g->pt_slots != slots || g->pt_slot_words != slot_words || g->pt_maxn != maxn)) {
+  if (g->pt_exec && (g->pt_slots != slots || g->pt_slot_words != slot_words || g->pt_maxn != maxn ||
+                     g->pt_cluster != cluster)) {
     cudaGraphExecDestroy(g->pt_exec);
     g->pt_exec = nullptr;
   }
   g->pt_off.assign(offsets, offsets + nparts + 1);
   g->pt_slots = slots;
+  g->pt_cluster = cluster;
   g->pt_slot_words = slot_words;
   g->pt_maxn = maxn;
   DAWN_CUDA(cudaStreamSynchronize(g->stream));
@@ -636,7 +642,7 @@ dawn_status parts_bfs(dawn_graph* g, const int32_t* source_offset, const int32_t
     cudaGraph_t graph = nullptr;
     cudaStream_t cs = g->stream;
     DAWN_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    parts_traverse<<<g->pt_slots, kPartBlock, 0, cs>>>(ctl, g->row_ptr, g->col, g->t_row_ptr, g->t_col, voff, scratch,
+    (g->pt_cluster == kPartCluster ? parts_traverse<kPartCluster> : parts_traverse<1>)<<<g->pt_slots, kPartBlock, 0, cs>>>(ctl, g->row_ptr, g->col, g->t_row_ptr, g->t_col, voff, scratch,
                                                   slot_words, maxn);
     const cudaError_t le = cudaGetLastError();
     const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
@@ -656,7 +662,7 @@ dawn_status parts_bfs(dawn_graph* g, const int32_t* source_offset, const int32_t
   if (g->pt_exec) {
     DAWN_CUDA(cudaGraphLaunch(g->pt_exec, g->stream));
   } else {
-    parts_traverse<<<g->pt_slots, kPartBlock, 0, g->stream>>>(ctl, g->row_ptr, g->col, g->t_row_ptr, g->t_col, voff,
+    (g->pt_cluster == kPartCluster ? parts_traverse<kPartCluster> : parts_traverse<1>)<<<g->pt_slots, kPartBlock, 0, g->stream>>>(ctl, g->row_ptr, g->col, g->t_row_ptr, g->t_col, voff,
                                                          scratch, slot_words, maxn);
     DAWN_CUDA(cudaGetLastError());
   }
