@@ -277,3 +277,42 @@ def test_deep_levels_written_directly(width):
                 bad = np.argwhere(d != want)
                 assert bad.size == 0, (g.n, width, force, bad[:5])
                 assert st.edges_traversed == edges
+
+
+def broom(mids=40, leaves=100, seed=0):
+    """Source 0 -> `mids` vertices -> `leaves` new leaves each -> one tail
+    vertex per leaf, undirected.  The second level discovers mids x leaves
+    vertices from rows shorter than 128 entries, more than one cluster CTA's
+    frontier slice holds, so the cluster levels spill and hand back."""
+    edges = []
+    nxt = 1 + mids
+    for i in range(mids):
+        edges.append((0, 1 + i))
+        for _ in range(leaves):
+            edges.append((1 + i, nxt))
+            nxt += 1
+    first_leaf, last_leaf = 1 + mids, nxt
+    for leaf in range(first_leaf, last_leaf):
+        edges.append((leaf, nxt))
+        nxt += 1
+    e = np.array(edges, np.int64)
+    e = np.concatenate([e, e[:, ::-1]])
+    rng = np.random.default_rng(seed)
+    w = rng.integers(1, 9, size=len(edges)).astype(np.int32)
+    w = np.concatenate([w, w])
+    order = np.lexsort((e[:, 1], e[:, 0]))
+    e, w = e[order], w[order]
+    rp = np.concatenate([[0], np.cumsum(np.bincount(e[:, 0], minlength=nxt))]).astype(np.int32)
+    return gen.CsrGraph(nxt, rp, e[:, 1].astype(np.int32), w, w.astype(np.float32), symmetric=True)
+
+
+def test_small_levels_slice_overflow():
+    g = broom()
+    srcs = np.array([0, 5], np.int32)
+    want, edges = expected(g, srcs)
+    with abi.Graph(g) as dg:
+        on, st_on = dg.bfs(srcs, variant=abi.VARIANT_DO)
+        dg.set_option(abi.OPT_SMALL_LEVELS, 0)
+        off, st_off = dg.bfs(srcs, variant=abi.VARIANT_DO)
+    assert np.array_equal(on, want) and np.array_equal(off, want)
+    assert st_on.edges_traversed == st_off.edges_traversed == edges

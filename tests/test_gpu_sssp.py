@@ -198,3 +198,18 @@ def test_small_levels_change_nothing():
                 bad = np.argwhere(to_ref(d) != want)
                 assert bad.size == 0, (g.n, wt, bad[:5])
             assert st_on.edges_traversed == st_off.edges_traversed
+
+
+def test_small_levels_slice_overflow():
+    # the broom of test_gpu_bfs: a cluster level finds more targets than a
+    # CTA's slice holds
+    from test_gpu_bfs import broom
+    g = broom(seed=85)
+    srcs = np.array([0, 5], np.int32)
+    want = O.msssp(g, srcs)
+    for wt in ("i32", "f32"):
+        with abi.Graph(g, weights=wt) as dg:
+            on, _ = dg.sssp(srcs, variant=abi.VARIANT_DO)
+            dg.set_option(abi.OPT_SMALL_LEVELS, 0)
+            off, _ = dg.sssp(srcs, variant=abi.VARIANT_DO)
+        assert np.array_equal(to_ref(on), want) and np.array_equal(to_ref(off), want), wt
