@@ -412,6 +412,33 @@ def suite_lines(torch, abi, gen, stream, rank):
             print(json.dumps(line), flush=True)
 
 
+def quick_multi(args, torch, abi, rank):
+    """--quick --graph er512: the multi-graph launch (512 uneven directed ER
+    graphs, 8-64 sources each) timed alone, for profiling."""
+    from dawn_gb300 import gen
+    graphs, gsrcs = gen.er_family(ngraphs=512, seed=GRAPH_SEED)
+    u, off = gen.disjoint_union(graphs)
+    s = torch.cuda.Stream()
+    torch.cuda.set_stream(s)
+    with abi.Graph(u, stream=s.cuda_stream) as dg:
+        dg.set_parts(off)
+        d = torch.empty(dg.multi_out_size(gsrcs), dtype=torch.int32, device="cuda")
+        for _ in range(args.warmup):
+            dg.multi_bfs_ptr(gsrcs, d.data_ptr(), device=True, stats=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            dg.multi_bfs_ptr(gsrcs, d.data_ptr(), device=True, stats=False)
+        e1.record()
+        torch.cuda.synchronize()
+        st = dg.multi_bfs_ptr(gsrcs, d.data_ptr(), device=True)
+        ms = e0.elapsed_time(e1) / max(1, args.steps)
+    if rank == 0:
+        print(json.dumps({"quick": True, "graph": "er512", "ms_per_step": round(ms, 4), "edges": st.edges_traversed,
+                          "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,8 +456,9 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner before the timed steps")
     ap.add_argument("--variant", default="bitset", choices=["bitset", "learned", "do", "push", "sssp", "sssp-single"],
                     help="--quick only: the traversal to run (sssp: batched weighted, int32 weights)")
-    ap.add_argument("--graph", default="rmat", choices=["rmat", "grid1024", "grid2048", "knn2M"],
-                    help="--quick only: rmat (of --scale), a 4-neighbour grid, or a k = 8 kNN graph on 2^21 points")
+    ap.add_argument("--graph", default="rmat", choices=["rmat", "grid1024", "grid2048", "knn2M", "er512"],
+                    help="--quick only: rmat (of --scale), a 4-neighbour grid, a k = 8 kNN graph on 2^21 points, "
+                         "or the 512 uneven ER graphs in one multi-graph launch")
     ap.add_argument("--sources", type=int, default=NSRC, help="--quick only: sources per step")
     ap.add_argument("--suite", action="store_true",
                     help="also time the other workload shapes (one JSON line each, before the main line)")
@@ -452,6 +480,8 @@ def main():
         _s = torch.cuda.Stream()
         torch.cuda.set_stream(_s)
         suite_lines(torch, abi, _gen, _s.cuda_stream, rank)
+    if args.quick and args.graph == "er512":
+        return quick_multi(args, torch, abi, rank)
     if args.quick and args.graph != "rmat":
         from dawn_gb300 import gen as _gen
         g = {"grid1024": lambda: _gen.grid(1024, 1024), "grid2048": lambda: _gen.grid(2048, 2048),
