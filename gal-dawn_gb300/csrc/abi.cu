@@ -151,6 +151,7 @@ void destroy(dawn_graph* g) {
   if (g->pt_exec) cudaGraphExecDestroy(g->pt_exec);
   if (g->mw_exec) cudaGraphExecDestroy(g->mw_exec);
   if (g->h_ctl) cudaFreeHost(g->h_ctl);
+  if (g->bc_h_level) cudaFreeHost(g->bc_h_level);
   for (cudaEvent_t e : g->trace_ev)
     if (e) cudaEventDestroy(e);
   if (g->ev0) cudaEventDestroy(g->ev0);

@@ -312,14 +312,19 @@ dawn_status prepare_heavy(dawn_graph* g) {
 
 dawn_status betweenness(dawn_graph* g, const int32_t* sources, int32_t nsrc, double* d_bc, dawn_stats* st) {
   const size_t nn = (size_t)g->n;
-  DAWN_CHECK(ensure(g->bc_levels, sizeof(int32_t) * kLanes * nn, g->stream));
+  // Level rows and ranges are double-buffered: the traversal of batch b runs
+  // while the host waits for batch b - 1's depth, so the stream always has
+  // work queued (traversal b, then the sweeps of b - 1).  The terms need one
+  // buffer: the amount and sweep passes of the batches follow one another.
+  DAWN_CHECK(ensure(g->bc_levels, sizeof(int32_t) * kLanes * nn * 2, g->stream));
   DAWN_CHECK(ensure(g->bc_terms, sizeof(float) * kLanes * nn, g->stream));
-  DAWN_CHECK(ensure(g->bc_range, sizeof(int32_t) * 2 * nn, g->stream));
+  DAWN_CHECK(ensure(g->bc_range, sizeof(int32_t) * 2 * nn * 2, g->stream));
   DAWN_CHECK(prepare_heavy(g));
+  if (!g->bc_h_level) DAWN_CUDA(cudaMallocHost(&g->bc_h_level, 2 * sizeof(int32_t)));
   DAWN_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * nn, g->stream));
-  int32_t* L = g->bc_levels.as<int32_t>();
+  int32_t* const Ls[2] = {g->bc_levels.as<int32_t>(), g->bc_levels.as<int32_t>() + kLanes * nn};
+  int32_t* const Rs[2] = {g->bc_range.as<int32_t>(), g->bc_range.as<int32_t>() + 2 * nn};
   float* T = g->bc_terms.as<float>();
-  int32_t* R = g->bc_range.as<int32_t>();
   const int32_t* hv = g->bc_heavy.as<int32_t>();
   HeavyRows hout{hv, hv + g->bc_hout, g->bc_hout, g->bc_segs_out};
   const int32_t* hin_base = hv + 2 * g->bc_hout + 1;
@@ -329,31 +334,56 @@ dawn_status betweenness(dawn_graph* g, const int32_t* sources, int32_t nsrc, dou
   const int grid = persistent_blocks((const void*)bc_sweep, kBlock, 0, g->blocks_per_sm);
   // the level pass runs the plain batched traversal (direction heuristic)
   DAWN_CHECK(call_selector(g, DAWN_VARIANT_BITSET, &g->sel_call));
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  dawn_status status = DAWN_OK;
   int64_t levels = 0;
-  for (int32_t b0 = 0; b0 < nsrc; b0 += kLanes) {
-    const int32_t k = nsrc - b0 < kLanes ? nsrc - b0 : kLanes;
-    int32_t deepest = 0;
-    DAWN_CHECK(bfs_bitset_levels(g, sources + b0, k, L, R, &deepest));
-    levels += deepest;
-    bc_amount<<<grid, kBlock, 0, g->stream>>>(g->t_row_ptr, g->t_col, L, T, g->n, hin, cnt);
-    DAWN_CUDA(cudaGetLastError());
-    if (hin.count) {
-      bc_amount_heavy<<<grid, kBlock, 0, g->stream>>>(L, T, hin, cnt);
-      DAWN_CUDA(cudaGetLastError());
+  const int32_t nb = (nsrc + kLanes - 1) / kLanes;
+  for (int i = 0; i < 2; i++)
+    if (cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming) != cudaSuccess) {
+      set_error("betweenness: cudaEventCreate failed");
+      status = DAWN_ERR_CUDA;
     }
+  for (int32_t b = 0; b <= nb && status == DAWN_OK; b++) {
+    if (b < nb) {
+      const int32_t b0 = b * kLanes, k = nsrc - b0 < kLanes ? nsrc - b0 : kLanes;
+      status = bfs_bitset_levels(g, sources + b0, k, Ls[b & 1], Rs[b & 1], g->bc_h_level + (b & 1));
+      if (status == DAWN_OK && cudaEventRecord(done[b & 1], g->stream) != cudaSuccess) {
+        set_error("betweenness: cudaEventRecord failed");
+        status = DAWN_ERR_CUDA;
+      }
+      if (status != DAWN_OK) break;
+    }
+    if (b == 0) continue;
+    // the dependency passes of batch b - 1, once its depth is known
+    const int p = (b - 1) & 1;
+    if (cudaEventSynchronize(done[p]) != cudaSuccess) {
+      set_error("betweenness: %s", cudaGetErrorString(cudaGetLastError()));
+      status = DAWN_ERR_CUDA;
+      break;
+    }
+    const int32_t deepest = g->bc_h_level[p] - 1;  // the batch ended on an empty level
+    levels += deepest;
+    const int32_t* L = Ls[p];
+    const int32_t* R = Rs[p];
+    bc_amount<<<grid, kBlock, 0, g->stream>>>(g->t_row_ptr, g->t_col, L, T, g->n, hin, cnt);
+    if (hin.count) bc_amount_heavy<<<grid, kBlock, 0, g->stream>>>(L, T, hin, cnt);
     for (int32_t l = deepest - 1; l >= 1; l--) {
       bc_sweep<<<grid, kBlock, 0, g->stream>>>(g->row_ptr, g->col, L, R, T, d_bc, g->n, l, hout, part);
-      DAWN_CUDA(cudaGetLastError());
-      if (hout.count) {
-        bc_sweep_heavy<<<grid, kBlock, 0, g->stream>>>(L, R, T, d_bc, l, hout, part);
-        DAWN_CUDA(cudaGetLastError());
-      }
+      if (hout.count) bc_sweep_heavy<<<grid, kBlock, 0, g->stream>>>(L, R, T, d_bc, l, hout, part);
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error("betweenness: %s", cudaGetErrorString(e));
+      status = DAWN_ERR_CUDA;
     }
   }
+  for (cudaEvent_t e : done)
+    if (e) cudaEventDestroy(e);
+  DAWN_CHECK(status);
   if (st) {
     std::memset(st, 0, sizeof(*st));
     st->levels = (int32_t)levels;
-    st->batches = (nsrc + kLanes - 1) / kLanes;
+    st->batches = nb;
   }
   return DAWN_OK;
 }

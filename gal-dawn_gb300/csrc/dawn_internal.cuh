@@ -190,6 +190,7 @@ struct dawn_graph {
   dawn::DevBuf bc_heavy;    // rows cut into segments: out-rows (ids, segment prefix), in-rows (same)
   dawn::DevBuf bc_part;     // per-segment partial sums (float) / per-heavy-row counts (int32), 64 each
   int32_t bc_hout = -1, bc_segs_out = 0, bc_hin = 0, bc_segs_in = 0;  // -1: lists not built
+  int32_t* bc_h_level = nullptr;  // pinned: the end level of the two batches in flight
   dawn::DevBuf mw_block;    // batched weighted traversal: n x 64 int32 distances
   dawn::DevBuf mw_masks;    // 3 x n uint64 improved-source masks
   dawn::DevBuf mw_ctl;
@@ -306,10 +307,11 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc,
                        unsigned long long* cc_cnt = nullptr);
 dawn_status bfs_bitset_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc);
 // One batch of at most 64 sources: levels as n x 64 int32 rows (vertex-major,
-// -1 unreached), per vertex the lowest and highest level (2 x n int32), and
-// the deepest level reached.
+// -1 unreached), per vertex the lowest and highest level (2 x n int32).
+// Enqueued only: the level the batch ended on (the deepest level + 1) is
+// copied to *h_level (pinned host memory) behind the traversal.
 dawn_status bfs_bitset_levels(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_levels,
-                              int32_t* d_range, int32_t* deepest);
+                              int32_t* d_range, int32_t* h_level);
 int bitset_width(const dawn_graph* g, int32_t nsrc);
 // govm.cu
 dawn_status sssp_single(dawn_graph* g, const int32_t* sources, int32_t nsrc,

@@ -1287,16 +1287,15 @@ dawn_status bfs_bitset(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
 }
 
 dawn_status bfs_bitset_levels(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32_t* d_levels,
-                              int32_t* d_range, int32_t* deepest) {
+                              int32_t* d_range, int32_t* h_level) {
   if (nsrc < 1 || nsrc > 64) {
     set_error("level mode takes 1 to 64 sources per call");
     return DAWN_ERR_INVALID_ARG;
   }
   DAWN_CHECK(run_width<1>(g, sources, nsrc, nullptr, nullptr, nullptr, d_levels, d_range));
-  BsCtl h;
-  DAWN_CUDA(cudaMemcpyAsync(&h, g->bs_ctl.p, sizeof(BsCtl), cudaMemcpyDeviceToHost, g->stream));
-  DAWN_CUDA(cudaStreamSynchronize(g->stream));
-  *deepest = h.level - 1;  // the batch ended on an empty level
+  // the level the batch ended on (an empty one), once the traversal is done
+  DAWN_CUDA(cudaMemcpyAsync(h_level, &g->bs_ctl.as<BsCtl>()->level, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                            g->stream));
   return DAWN_OK;
 }
 
