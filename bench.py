@@ -55,11 +55,32 @@ def dist_env():
     return ws, rank, local
 
 
+def rank_sources(g, rank):
+    """The sources a rank traverses: every rank its own seeded draw of NSRC
+    (the path shards by source; no rank waits on another's data)."""
+    from dawn_gb300 import gen
+    return gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
+
+
+def aggregate(torch, ms_step, edges, ws, device):
+    """Whole-job figures over the ranks: the slowest rank's step time and
+    the edges all ranks traversed.  `device` is where the reduction runs
+    ("cuda" under NCCL, "cpu" under gloo)."""
+    t = torch.tensor([float(ms_step)], dtype=torch.float64, device=device)
+    e = torch.tensor([int(edges)], dtype=torch.int64, device=device)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(e, op=torch.distributed.ReduceOp.SUM)
+    ms = float(t.item())
+    total = int(e.item())
+    return ms, total, total / (ms * 1e-3) / 1e9
+
+
 def make_workload(scale, rank, weighted=False):
     from dawn_gb300 import gen
     t = time.time()
     g = gen.rmat(scale, EDGEFACTOR, A, B, C, seed=GRAPH_SEED, weights=weighted)
-    srcs = gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
+    srcs = rank_sources(g, rank)
     log(f"[bench] rmat{scale}: n={g.n} m={g.m} generated in {time.time() - t:.1f}s")
     return g, srcs
 
@@ -552,13 +573,8 @@ def main():
     clocks.start()
     ms = time_steps(torch, step, args.steps, args.warmup, barrier)
     clk = clocks.stop()
-    ms_step = ms / args.steps
-    # max over ranks
-    t = torch.tensor([ms_step], device="cuda")
-    if ws > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_step = float(t.item())
-    value = edges * ws / (ms_step * 1e-3) / 1e9
+    # the slowest rank's time, the edges of all ranks
+    ms_step, _, value = aggregate(torch, ms / args.steps, edges, ws, "cuda")
 
     # plain single-source direction-optimising kernels, same sources
     step_plain = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_DO, stats=False)  # noqa
@@ -618,9 +634,10 @@ def main():
         e2e_step(record=True)
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+    e2e_ms, _, e2e_gteps = aggregate(torch, e2e_ms, edges, ws, "cuda")
     h2d = 4 * (g.n + 1) + 4 * g.m + 4 * NSRC
     d2h = 4 * NSRC * g.n
-    e2e = {"value": round(edges / (e2e_ms * 1e-3) / 1e9 * ws, 3), "unit": "GTEPS", "ms_per_step": round(e2e_ms, 3),
+    e2e = {"value": round(e2e_gteps, 3), "unit": "GTEPS", "ms_per_step": round(e2e_ms, 3),
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
            "phases_ms": {k: round(v / args.e2e_steps, 3) for k, v in phases.items()},
            "call": "dawn_graph_create(pinned host CSR) + dawn_bfs(pinned host dist) + dawn_graph_destroy"}
