@@ -38,13 +38,14 @@ namespace {
 
 constexpr int kBatch = 64;  // sources per batch (two per lane)
 constexpr int kUnroll = 4;  // edges whose distance rows are fetched together
+constexpr int kInitBlock = 1024;  // threads per source in mw_init (hub rows)
 
 struct MwCtl {
   int32_t qsize[2];
   unsigned long long lpack[2];
   unsigned long long mf[2];
   int32_t level, done, batch, nsrc;
-  int32_t n_push, pad0;
+  int32_t n_push, inits;       // inits: mw_init CTAs finished
   unsigned long long reached;   // TEPS numerator of all batches so far
   int32_t* dist_base;           // nsrc x n output (source-major)
   const int32_t* sources;
@@ -56,8 +57,20 @@ __device__ __forceinline__ int32_t relax(int32_t d, int32_t w, bool is_float) {
   return d + w;
 }
 
-__global__ void __launch_bounds__(kBlock) mw_clear(int32_t* __restrict__ D, size_t words, int32_t inf,
-                                                   unsigned long long* __restrict__ masks, size_t nmask) {
+// Fills the block with "unreached", clears the mask slots and resets the
+// level counters for the batch.
+__global__ void __launch_bounds__(kBlock) mw_clear(MwCtl* __restrict__ ctl, int32_t* __restrict__ D, size_t words,
+                                                   int32_t inf, unsigned long long* __restrict__ masks,
+                                                   size_t nmask) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->qsize[0] = ctl->qsize[1] = 0;
+    ctl->lpack[0] = ctl->lpack[1] = 0;
+    ctl->mf[0] = ctl->mf[1] = 0;
+    ctl->level = 1;
+    ctl->done = 0;
+    ctl->n_push = 0;
+    ctl->inits = 0;
+  }
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   int4* d4 = reinterpret_cast<int4*>(D);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < words / 4; i += stride)
@@ -65,37 +78,33 @@ __global__ void __launch_bounds__(kBlock) mw_clear(int32_t* __restrict__ D, size
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nmask; i += stride) masks[i] = 0ull;
 }
 
-// One CTA: the batch's sources one after another.  For source b, each
-// distinct neighbour takes the weight of its last CSR entry (an atomicMax
-// on the entry position picks it), enters the level-0 mask with bit b and
-// is queued by its first setter; then the source's own entry is set to 0.
-__global__ void __launch_bounds__(1024) mw_init(MwCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
-                                                const int32_t* __restrict__ col, const int32_t* __restrict__ w,
-                                                int32_t* __restrict__ D, unsigned long long* __restrict__ mask0,
-                                                unsigned long long* __restrict__ last, int32_t* __restrict__ q,
-                                                Seg* __restrict__ segs, int32_t n) {
+// One CTA per source b of the batch (kBatch CTAs; those past the batch's
+// end only check in).  Each distinct neighbour takes the weight of its last
+// CSR entry: the entries first lower the neighbour's block word for b to
+// -(k + 1) with atomicMin, so the largest position k wins, and the winner
+// then stores its weight there (weights are non-negative, so no later test
+// mistakes a weight for a marker).  Column b of the block is this CTA's
+// alone.  A winner enters the level-0 mask with bit b and is queued by its
+// first setter; then the source's own entry is set to 0.  The last CTA to
+// check in decides whether the first frontier is empty.
+__global__ void __launch_bounds__(kInitBlock) mw_init(MwCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
+                                                      const int32_t* __restrict__ col,
+                                                      const int32_t* __restrict__ w, int32_t* __restrict__ D,
+                                                      unsigned long long* __restrict__ mask0,
+                                                      int32_t* __restrict__ q, Seg* __restrict__ segs) {
   const int batch = ctl->batch;
   const int nb = min(kBatch, ctl->nsrc - batch * kBatch);
-  if (threadIdx.x == 0) {
-    ctl->qsize[0] = ctl->qsize[1] = 0;
-    ctl->lpack[0] = ctl->lpack[1] = 0;
-    ctl->mf[0] = ctl->mf[1] = 0;
-    ctl->level = 1;
-    ctl->done = 0;
-    ctl->n_push = 0;
-  }
-  __syncthreads();
-  for (int b = 0; b < nb; b++) {
+  const int b = blockIdx.x;
+  if (b < nb) {
     const int32_t s = ctl->sources[batch * kBatch + b];
     const int rs = row_ptr[s], re = row_ptr[s + 1];
-    for (int k = rs + threadIdx.x; k < re; k += blockDim.x) last[col[k]] = 0;
-    __syncthreads();
-    for (int k = rs + threadIdx.x; k < re; k += blockDim.x) atomicMax(last + col[k], (unsigned long long)(k + 1));
+    for (int k = rs + threadIdx.x; k < re; k += blockDim.x) atomicMin(D + (size_t)col[k] * kBatch + b, -(k + 1));
     __syncthreads();
     for (int k = rs + threadIdx.x; k < re; k += blockDim.x) {
       const int32_t u = col[k];
-      if (last[u] != (unsigned long long)(k + 1)) continue;
-      D[(size_t)u * kBatch + b] = __ldg(w + k);
+      int32_t* du = D + (size_t)u * kBatch + b;
+      if (__ldcg(du) != -(k + 1)) continue;
+      *du = __ldg(w + k);
       const unsigned long long old = atomicOr(mask0 + u, 1ull << b);
       if (old == 0ull) {
         const int urs = row_ptr[u], udeg = row_ptr[u + 1] - urs;
@@ -111,9 +120,15 @@ __global__ void __launch_bounds__(1024) mw_init(MwCtl* __restrict__ ctl, const i
     }
     __syncthreads();
     if (threadIdx.x == 0) D[(size_t)s * kBatch + b] = 0;
-    __syncthreads();
   }
-  if (threadIdx.x == 0) ctl->done = ctl->qsize[0] == 0 && ctl->lpack[0] == 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ctl->inits, 1) == (int)gridDim.x - 1) {
+      __threadfence();
+      ctl->done = __ldcg(&ctl->qsize[0]) == 0 && __ldcg(&ctl->lpack[0]) == 0ull;
+    }
+  }
 }
 
 // The row [k0, k1) of frontier vertex u relaxed by one warp: lane i owns
@@ -348,31 +363,59 @@ __global__ void mw_decide(MwCtl* __restrict__ ctl, int32_t n, cudaGraphCondition
 }
 
 // Block -> the batch's source-major rows; each vertex adds its out-degree
-// once per source that reached it (TEPS numerator).
-__global__ void __launch_bounds__(kBlock) mw_emit(MwCtl* __restrict__ ctl, const int32_t* __restrict__ D,
-                                                  const int32_t* __restrict__ row_ptr, int32_t inf, int32_t n) {
+// once per source that reached it (TEPS numerator).  A warp takes 32
+// consecutive vertices: their 32 rows are 8 KB of the block in one piece,
+// read with coalesced 16-byte loads (512 bytes per warp load, all sixteen
+// issued before the first is waited on), transposed through a padded
+// shared-memory tile and written as one 128-byte run per source row.
+constexpr int kEmitBlock = 128;
+constexpr int kEmitPitch = kBatch + 1;  // words per tile row: column reads hit 32 banks
+
+__global__ void __launch_bounds__(kEmitBlock) mw_emit(MwCtl* __restrict__ ctl, const int32_t* __restrict__ D,
+                                                      const int32_t* __restrict__ row_ptr, int32_t inf, int32_t n) {
+  __shared__ int32_t s_tile[kEmitBlock / 32][32 * kEmitPitch];
   const int batch = ctl->batch;
   const int nb = min(kBatch, ctl->nsrc - batch * kBatch);
   int32_t* dist = ctl->dist_base + (size_t)batch * kBatch * n;
+  int32_t* tile = s_tile[threadIdx.x >> 5];
+  const int lane = lane_id();
+  constexpr int kVecs = 32 * kBatch / 4;  // 16-byte pieces of 32 rows
   unsigned long long reached = 0;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < (size_t)n; v += stride) {
-    const int4* row = reinterpret_cast<const int4*>(D + v * kBatch);
-    int cnt = 0;
-    for (int c = 0; c < nb; c += 4) {
-      const int4 x = __ldcs(row + c / 4);
-      const int32_t xs[4] = {x.x, x.y, x.z, x.w};
+  const size_t nwarps = (size_t)gridDim.x * (kEmitBlock / 32);
+  for (size_t v0 = ((size_t)blockIdx.x * (kEmitBlock / 32) + (threadIdx.x >> 5)) * 32; v0 < (size_t)n;
+       v0 += nwarps * 32) {
+    const int rows = (int)min((size_t)32, (size_t)n - v0);
+    const int4* src = reinterpret_cast<const int4*>(D + v0 * kBatch);
+    int4 x[kVecs / 32];
 #pragma unroll
-      for (int j = 0; j < 4; j++)
-        if (c + j < nb) {
-          dist[(size_t)(c + j) * n + v] = xs[j];
-          cnt += xs[j] != inf;
-        }
+    for (int i = 0; i < kVecs / 32; i++) {
+      const int j = i * 32 + lane;  // piece j: row j / 16, words 4 (j % 16) ..
+      x[i] = j / (kBatch / 4) < rows ? __ldcs(src + j) : make_int4(inf, inf, inf, inf);
     }
-    reached += (unsigned long long)cnt * (unsigned long long)(row_ptr[v + 1] - row_ptr[v]);
+#pragma unroll
+    for (int i = 0; i < kVecs / 32; i++) {
+      const int j = i * 32 + lane;
+      int32_t* t = tile + (j / (kBatch / 4)) * kEmitPitch + (j % (kBatch / 4)) * 4;
+      t[0] = x[i].x;
+      t[1] = x[i].y;
+      t[2] = x[i].z;
+      t[3] = x[i].w;
+    }
+    __syncwarp();
+    int cnt = 0;
+    const bool own = lane < rows;
+    for (int c = 0; c < nb; c++) {
+      const int32_t d = tile[lane * kEmitPitch + c];
+      if (own) {
+        dist[(size_t)c * n + v0 + lane] = d;
+        cnt += d != inf;
+      }
+    }
+    if (own) reached += (unsigned long long)cnt * (unsigned long long)(row_ptr[v0 + lane + 1] - row_ptr[v0 + lane]);
+    __syncwarp();
   }
   reached = warp_sum(reached);
-  if (lane_id() == 0 && reached) atomicAdd(&ctl->reached, reached);
+  if (lane == 0 && reached) atomicAdd(&ctl->reached, reached);
 }
 
 __global__ void mw_next(MwCtl* __restrict__ ctl) {
@@ -404,7 +447,6 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
   DAWN_CHECK(ensure(g->mw_masks, sizeof(unsigned long long) * 3 * nn, g->stream));
   DAWN_CHECK(ensure(g->ss_queues, sizeof(int32_t) * 2 * nn, g->stream));
   DAWN_CHECK(ensure(g->ss_segs, sizeof(Seg) * 2 * segcap, g->stream));
-  DAWN_CHECK(ensure(g->ss_scratch, sizeof(unsigned long long) * nn, g->stream));
   DAWN_CHECK(ensure(g->mw_ctl, sizeof(MwCtl), g->stream));
   DAWN_CHECK(ensure(g->mw_sources, sizeof(int32_t) * (size_t)nsrc, g->stream));
   DAWN_CUDA(cudaMemcpyAsync(g->mw_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
@@ -420,7 +462,7 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
     const int32_t *row_ptr, *col, *w;
     int is_float;
     int32_t* D;
-    unsigned long long *masks, *last;
+    unsigned long long* masks;
     int32_t* q;
     Seg* segs;
     size_t segcap, words, nmask;
@@ -435,7 +477,6 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
   a.is_float = is_float;
   a.D = g->mw_block.as<int32_t>();
   a.masks = g->mw_masks.as<unsigned long long>();
-  a.last = g->ss_scratch.as<unsigned long long>();
   a.q = g->ss_queues.as<int32_t>();
   a.segs = g->ss_segs.as<Seg>();
   a.segcap = segcap;
@@ -445,8 +486,8 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
   a.inf = is_float ? 0x7f7fffff : 0x7fffffff;  // FLT_MAX bits / INT32_MAX
   a.handle = 0;
   a.in_graph = 0;
-  void* clear_args[] = {&a.D, &a.words, &a.inf, &a.masks, &a.nmask};
-  void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.w, &a.D, &a.masks, &a.last, &a.q, &a.segs, &a.n};
+  void* clear_args[] = {&a.ctl, &a.D, &a.words, &a.inf, &a.masks, &a.nmask};
+  void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.w, &a.D, &a.masks, &a.q, &a.segs};
   void* push_args[] = {&a.row_ptr, &a.col, &a.w, &a.is_float, &a.ctl, &a.D, &a.masks, &a.q, &a.segs, &a.segcap,
                        &a.n};
   void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
@@ -456,14 +497,14 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
   SsFamily fam;
   fam.npre = 2;
   fam.pre[0] = {(const void*)mw_clear, clear_args, dim3(sms * 8), dim3(kBlock), "mw_clear"};
-  fam.pre[1] = {(const void*)mw_init, init_args, dim3(1), dim3(1024), "mw_init"};
+  fam.pre[1] = {(const void*)mw_init, init_args, dim3(kBatch), dim3(kInitBlock), "mw_init"};
   fam.nbody = 2;
   fam.body[0] = {(const void*)mw_push, push_args,
                  dim3(persistent_blocks((const void*)mw_push, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
                  "mw_push", kModePush};
   fam.body[1] = {(const void*)mw_decide, decide_args, dim3(1), dim3(32), "mw_decide"};
   fam.npost = 2;
-  fam.post[0] = {(const void*)mw_emit, emit_args, dim3(sms * 8), dim3(kBlock), "mw_emit"};
+  fam.post[0] = {(const void*)mw_emit, emit_args, dim3(sms * 8), dim3(kEmitBlock), "mw_emit"};
   fam.post[1] = {(const void*)mw_next, next_args, dim3(1), dim3(32), "mw_next"};
   fam.ctl = a.ctl;
   fam.ctl_bytes = sizeof(MwCtl);
