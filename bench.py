@@ -477,8 +477,9 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner before the timed steps")
     ap.add_argument("--variant", default="bitset", choices=["bitset", "learned", "do", "push", "sssp", "sssp-single"],
                     help="--quick only: the traversal to run (sssp: batched weighted, int32 weights)")
-    ap.add_argument("--graph", default="rmat", choices=["rmat", "grid1024", "grid2048", "knn2M", "er512"],
+    ap.add_argument("--graph", default="rmat", choices=["rmat", "grid1024", "grid2048", "knn2M", "er64k", "er512"],
                     help="--quick only: rmat (of --scale), a 4-neighbour grid, a k = 8 kNN graph on 2^21 points, "
+                         "the directed ER graph of 65,536 vertices and 2^20 edges, "
                          "or the 512 uneven ER graphs in one multi-graph launch")
     ap.add_argument("--sources", type=int, default=NSRC, help="--quick only: sources per step")
     ap.add_argument("--suite", action="store_true",
@@ -506,8 +507,12 @@ def main():
     if args.quick and args.graph != "rmat":
         from dawn_gb300 import gen as _gen
         g = {"grid1024": lambda: _gen.grid(1024, 1024), "grid2048": lambda: _gen.grid(2048, 2048),
-             "knn2M": lambda: _gen.knn(1 << 21, 8, seed=GRAPH_SEED)}[args.graph]()
-        srcs = _gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
+             "knn2M": lambda: _gen.knn(1 << 21, 8, seed=GRAPH_SEED),
+             "er64k": lambda: _gen.erdos_renyi(65536, 1 << 20, seed=1)}[args.graph]()
+        if args.graph == "er64k":  # the suite's sources for this graph
+            srcs = _gen.sources(g, NSRC, seed=2, from_lcc=False)
+        else:
+            srcs = _gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
     else:
         g, srcs = make_workload(args.scale, rank, weighted=args.quick and args.variant.startswith("sssp"))
     if args.quick:

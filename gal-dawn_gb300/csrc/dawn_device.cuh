@@ -82,15 +82,22 @@ constexpr int kWarpRow = 32;  // rows with at least this many entries use the wh
 // the row of vertex v.  s_excl / s_rs / s_v are this warp's 32-entry
 // shared-memory scratch.  kCoherent reads the queue through L2 (a queue
 // written earlier in the same launch must not come from the read-only path).
+// A warp task is 32 queue entries, or fewer when the queue cannot give every
+// warp 32: the smallest power of two that still covers the queue in one
+// round of the grid, so a short queue is spread over all warps instead of
+// being walked by a few (64 rows of 16 edges: 64 warps, not two).
 template <bool kCoherent = false, class Op>
 __device__ __forceinline__ void warp_expand(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ qin,
                                             int qn, int* s_excl, int* s_rs, int* s_v, Op&& op) {
   const int lane = lane_id();
-  for (int base = global_warp() * 32; base < qn; base += num_warps() * 32) {
+  const int nw = num_warps();
+  int per = 32;
+  while (per > 1 && (long long)(per >> 1) * nw >= qn) per >>= 1;
+  for (int base = global_warp() * per; base < qn; base += nw * per) {
     const int idx = base + lane;
     int32_t v = -1;
     int rs = 0, re = 0;
-    if (idx < qn) {
+    if (lane < per && idx < qn) {
       v = kCoherent ? __ldcg(qin + idx) : qin[idx];
       rs = row_ptr[v];
       re = row_ptr[v + 1];
