@@ -407,11 +407,10 @@ struct LevelAcc {
 // the warp finishing a row's last segment folds the accumulator into the
 // vertex, so only one warp writes a vertex's words and every segment sees
 // the same visited words for the whole level.  Light rows follow, 32 list
-// entries per warp task from a shared counter: rows of >= 32 entries are
-// swept by the whole warp (4 gathers in flight per lane, early exit once no
-// missing bit is left), shorter ones are concatenated across the warp and
-// OR-ed into per-lane shared-memory slots.  The list is filtered into the
-// next unfinished list as it goes.
+// entries per warp task from a shared counter: rows of >= kPullLaneMax
+// entries are swept by the whole warp (4 gathers in flight per lane, early
+// exit once no missing bit is left), shorter ones are walked by one lane
+// each.  The list is filtered into the next unfinished list as it goes.
 template <int W>
 __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t* __restrict__ row_ptr,
                                                      const int32_t* __restrict__ t_row_ptr,
