@@ -155,13 +155,15 @@ __device__ __forceinline__ void push_level(int* s_excl, int* s_rs, int* s_v, int
       if (u != source) {
         const int32_t nd = relax_sum(__ldcg(dist + v), k, wi, wf, is_float != 0);
         if (nd < __ldcg(dist + u)) {
-          const int32_t old = atomicMin(dist + u, nd);
-          if (nd < old) {
-            // the target was just lowered, so its bit is rarely set yet:
-            // claim it with the OR alone, without a look first
-            const uint32_t bit = 1u << (u & 31);
-            found = !(atomicOr(inq_out + (u >> 5), bit) & bit);
-          }
+          // Improvement is judged against the distance just read, and the
+          // minimum is a reduction without a return value (no round trip):
+          // a target another warp lowered further in the meantime is only
+          // queued once more, and its next expansion relaxes nothing new.
+          // The target was just lowered, so its bit is rarely set yet:
+          // claim it with the OR alone, without a look first.
+          atomicMin(dist + u, nd);
+          const uint32_t bit = 1u << (u & 31);
+          found = !(atomicOr(inq_out + (u >> 5), bit) & bit);
         }
       }
     }
