@@ -632,6 +632,13 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
                   segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
   clear_next_slice<W>(slices, n, L, ctl->nbits);
   const int wib = threadIdx.x >> 5;
+  // The first two levels expand the sources and their neighbours, whose
+  // targets are almost never visited yet: there the visited words are not
+  // read (one random load per edge fewer), and the update drops the few
+  // visited bits.  Later levels filter first, which saves the atomics of
+  // edges back into the visited region (half of a wavefront's edges on a
+  // mesh).
+  const bool filter = L > 2;
   WarpQueue wq(s_q[wib], tq, &ctl->tq_size);
   auto op = [&](int32_t v, int k, bool valid) {
     bool first = false;
@@ -641,7 +648,8 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
       // No look at `next` first: its bits are OR-ed in whether or not they
       // are there, which saves a random load per edge (the scatter is bound
       // by the L1/TEX traffic of its random accesses).
-      const B bits = B::ldg(fin + (size_t)v * W).andnot(B::ldcg(visit + (size_t)u * W));
+      B bits = B::ldg(fin + (size_t)v * W);
+      if (filter) bits = bits.andnot(B::ldcg(visit + (size_t)u * W));
       if (bits.any()) {
         if (W == 1 && !dense) {
           // one word: the OR that finds it empty is the first touch (no
