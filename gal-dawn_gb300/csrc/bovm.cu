@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
-  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueueBig];
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
 
   unsigned long long my_mf = 0;
-  WarpQueue wq(s_q[wib], qout, qcount);
+  WarpQueueBig wq(s_q[wib], qout, qcount);
   auto op = [&](int32_t, int k, bool valid) {
     const int32_t u = valid ? __ldg(col + k) : -1;
     const bool found = valid && claim_bit(vbm, u);
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
                                                    int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
                                                    uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
                                                    int32_t n, int32_t nwords) {
-  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueueBig];
   if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
   const int pout = L & 1;
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
 
   unsigned long long my_mf = 0;
-  WarpQueue wq(s_q[threadIdx.x >> 5], qout, qcount);
+  WarpQueueBig wq(s_q[threadIdx.x >> 5], qout, qcount);
   for (int w = global_warp(); w < nwords; w += num_warps()) {
     const uint32_t vis = vbm[w];
     uint32_t unv = ~vis;

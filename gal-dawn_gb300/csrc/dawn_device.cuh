@@ -233,18 +233,24 @@ namespace dawn {
 // Per-warp staging of queue appends in shared memory.  Appending straight
 // to a global queue costs one atomicAdd on the queue's single counter per
 // warp step; with thousands of warps those same-address atomics serialise.
-// Here a warp collects up to kWarpQueue entries (warp-synchronously, no
-// atomics) and reserves global space once per full buffer.  All 32 lanes
-// must make every call; flush() must run before the warp exits.
+// Here a warp collects up to kCap entries (warp-synchronously, no atomics)
+// and reserves global space once per full buffer.  All 32 lanes must make
+// every call; flush() must run before the warp exits.  The unweighted
+// traversals stage kWarpQueueBig entries (a quarter of the counter's
+// atomics: RMAT-22 x 64 batched 1.66 -> 1.64 ms, 64 single-source
+// traversals 18.0 -> 17.5 ms); the batched min-plus kernel lost 4.5% with
+// the larger buffer and keeps kWarpQueue.
 constexpr int kWarpQueue = 64;
+constexpr int kWarpQueueBig = 256;
 
-struct WarpQueue {
-  int32_t* buf;      // this warp's kWarpQueue shared-memory slots
+template <int kCap = kWarpQueue>
+struct WarpQueueT {
+  int32_t* buf;      // this warp's kCap shared-memory slots
   int32_t* out;      // global queue
   int32_t* count;    // global queue length
   int n = 0;         // staged entries (warp-uniform)
 
-  __device__ __forceinline__ WarpQueue(int32_t* sbuf, int32_t* q, int32_t* cnt) : buf(sbuf), out(q), count(cnt) {}
+  __device__ __forceinline__ WarpQueueT(int32_t* sbuf, int32_t* q, int32_t* cnt) : buf(sbuf), out(q), count(cnt) {}
 
   __device__ __forceinline__ void flush() {
     if (n == 0) return;
@@ -261,14 +267,18 @@ struct WarpQueue {
     const uint32_t m = __ballot_sync(kFull, pred);
     if (m == 0) return;
     const int c = __popc(m);
-    if (n + c > kWarpQueue) flush();
+    if (n + c > kCap) flush();
     if (pred) buf[n + __popc(m & lanemask_lt())] = v;
     n += c;
   }
 };
 
-// emit_routed with the short-row queue staged through a WarpQueue.
-__device__ __forceinline__ void emit_routed(bool found, int32_t u, int deg, int rs, WarpQueue& q_short,
+using WarpQueue = WarpQueueT<>;
+using WarpQueueBig = WarpQueueT<kWarpQueueBig>;
+
+// emit_routed with the short-row queue staged through a WarpQueueT.
+template <int kCap>
+__device__ __forceinline__ void emit_routed(bool found, int32_t u, int deg, int rs, WarpQueueT<kCap>& q_short,
                                             Seg* __restrict__ segs, unsigned long long* lpack) {
   const bool is_long = found && deg >= kLongRow;
   q_short.push(found && !is_long, u);

@@ -423,8 +423,8 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
                                                      const int32_t* __restrict__ hv_segoff, u64* __restrict__ hv_acc,
                                                      int32_t hv_count, int32_t hv_segs, int32_t pull_seg, int32_t n) {
   using B = Bits<W>;
-  __shared__ int32_t s_qa[kBlock / 32][kWarpQueue];
-  __shared__ int32_t s_qu[kBlock / 32][kWarpQueue];
+  __shared__ int32_t s_qa[kBlock / 32][kWarpQueueBig];
+  __shared__ int32_t s_qu[kBlock / 32][kWarpQueueBig];
   if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
   const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n * W;
@@ -445,8 +445,8 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
   const B full = B::full_of(ctl);
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   LevelAcc acc;
-  WarpQueue qa(s_qa[wib], aq_out, aq_count);
-  WarpQueue qu(s_qu[wib], ul_out, ul_count);
+  WarpQueueBig qa(s_qa[wib], aq_out, aq_count);
+  WarpQueueBig qu(s_qu[wib], ul_out, ul_count);
   const bool deep_cc = ctl->cc_sum && L >= kDeepLevel;
 
   for (;;) {
@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
   __shared__ int s_excl[kBlock / 32][32];
   __shared__ int s_rs[kBlock / 32][32];
   __shared__ int s_v[kBlock / 32][32];
-  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueueBig];
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n * W;
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
   // edges back into the visited region (half of a wavefront's edges on a
   // mesh).
   const bool filter = L > 2;
-  WarpQueue wq(s_q[wib], tq, &ctl->tq_size);
+  WarpQueueBig wq(s_q[wib], tq, &ctl->tq_size);
   auto op = [&](int32_t v, int k, bool valid) {
     bool first = false;
     int32_t u = -1;
@@ -683,7 +683,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
                                                          const int32_t* __restrict__ tq, uint32_t* __restrict__ tbm,
                                                          int32_t n) {
   using B = Bits<W>;
-  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueueBig];
   if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   u64* __restrict__ fout = fr + (size_t)(L % 3) * n * W;
@@ -692,7 +692,7 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
   const B full = B::full_of(ctl);
   const bool dense = ctl->dense != 0;
   const int tn = dense ? n : ctl->tq_size;
-  WarpQueue wq(s_q[threadIdx.x >> 5], aq_out, &ctl->aq_size[L % 3]);
+  WarpQueueBig wq(s_q[threadIdx.x >> 5], aq_out, &ctl->aq_size[L % 3]);
   LevelAcc acc;
   const bool deep_cc = ctl->cc_sum && L >= kDeepLevel;
   const int total = gridDim.x * blockDim.x;
