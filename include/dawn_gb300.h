@@ -317,8 +317,8 @@ dawn_status dawn_graph_get_option(const dawn_graph* g, int32_t option,
  * smallest prediction when it beats the direction heuristic's choice by
  * DAWN_OPT_SELECTOR_MARGIN, else the heuristic's choice: the heuristic is
  * both the fallback and the reference the selector must beat.  weights =
- * NULL (count 0) restores the
- * heuristics alone.  Distances never depend on the choice. */
+ * NULL (count 0) restores the heuristics alone.  Distances never depend on
+ * the choice. */
 #define DAWN_SELECTOR_WEIGHTS 1475
 dawn_status dawn_graph_set_selector(dawn_graph* g, const float* weights,
                                     int32_t count);
