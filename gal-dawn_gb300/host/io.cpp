@@ -16,10 +16,16 @@
 // line is skipped (the reference re-reads the previous line's column), an
 // index outside the matrix is an error, and a weighted read of a line
 // without a value uses weight 1.
+// Opt-in, not in the reference: DAWN_DEDUP=1 drops repeated (row, col)
+// entries of an unweighted read (hop distances do not depend on them; the
+// edge count and the TEPS numerator then count each edge once).  Weighted
+// reads keep them, because the source-row rule (the last repeated entry's
+// weight) makes distances depend on the repeats.
 #include <dawn/io.hxx>
 
 #include <sys/stat.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <parallel/algorithm>
 #include <tuple>
@@ -141,7 +147,12 @@ std::vector<Entry> parse_entries(const std::string& text, bool weighted, int row
   return all;
 }
 
-void build(DAWN::Graph::Graph_t& graph, std::vector<Entry>& e, bool symmetric, bool weighted) {
+bool dedup_requested() {
+  const char* env = std::getenv("DAWN_DEDUP");
+  return env && *env && std::string(env) != "0";
+}
+
+void build(DAWN::Graph::Graph_t& graph, std::vector<Entry>& e, bool symmetric, bool weighted, bool dedup) {
   if (symmetric) {
     const size_t k = e.size();
     e.resize(2 * k);
@@ -156,6 +167,10 @@ void build(DAWN::Graph::Graph_t& graph, std::vector<Entry>& e, bool symmetric, b
 #pragma omp parallel for
     for (size_t i = 0; i < e.size(); i++) key[i] = ((uint64_t)(uint32_t)e[i].r << 32) | (uint32_t)e[i].c;
     __gnu_parallel::sort(key.begin(), key.end());
+    if (dedup) {
+      key.erase(std::unique(key.begin(), key.end()), key.end());
+      e.resize(key.size());
+    }
 #pragma omp parallel for
     for (size_t i = 0; i < e.size(); i++) e[i] = Entry{(int)(key[i] >> 32), (int)(uint32_t)key[i], 0.0f};
   }
@@ -186,7 +201,7 @@ void build(DAWN::Graph::Graph_t& graph, std::vector<Entry>& e, bool symmetric, b
 // Parsing a large MatrixMarket file dominates a tool's run time; the CSR it
 // yields depends only on the file and on the reader (symmetric or directed,
 // weighted or not).  With DAWN_CSR_CACHE set, the CSR is stored after the
-// first parse as <file name>.<s|d><w|u>.dawncsr, beside the input file
+// first parse as <file name>.<s|d><w|u>[x].dawncsr (x: DAWN_DEDUP), beside the input file
 // (DAWN_CSR_CACHE=1) or in the directory the variable names, together with
 // the input's size and modification time; a later load of the same,
 // unchanged file with the same reader reads the arrays back instead.  A
@@ -202,7 +217,7 @@ struct CacheHeader {
 };
 constexpr char kCacheMagic[8] = {'D', 'A', 'W', 'N', 'C', 'S', 'R', '1'};
 
-std::string cache_path(const std::string& input, bool symmetric, bool weighted) {
+std::string cache_path(const std::string& input, bool symmetric, bool weighted, bool dedup) {
   const char* env = std::getenv("DAWN_CSR_CACHE");
   if (!env || !*env || std::string(env) == "0") return "";
   std::string name = input;
@@ -212,7 +227,7 @@ std::string cache_path(const std::string& input, bool symmetric, bool weighted) 
     name = slash == std::string::npos ? input : input.substr(slash + 1);
     dir = std::string(env) + "/";
   }
-  return dir + name + "." + (symmetric ? "s" : "d") + (weighted ? "w" : "u") + ".dawncsr";
+  return dir + name + "." + (symmetric ? "s" : "d") + (weighted ? "w" : "u") + (dedup ? "x" : "") + ".dawncsr";
 }
 
 bool source_stat(const std::string& input, int64_t* size, int64_t* mtime_ns) {
@@ -224,14 +239,14 @@ bool source_stat(const std::string& input, int64_t* size, int64_t* mtime_ns) {
 }
 
 bool load_cache(const std::string& cpath, const std::string& input, DAWN::Graph::Graph_t& graph, bool symmetric,
-                bool weighted) {
+                bool weighted, bool dedup) {
   int64_t size = 0, mtime = 0;
   if (!source_stat(input, &size, &mtime)) return false;
   FILE* f = std::fopen(cpath.c_str(), "rb");
   if (!f) return false;
   CacheHeader h;
   bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kCacheMagic, 8) == 0 && h.version == 1 &&
-            h.flags == (uint32_t)((symmetric ? 1 : 0) | (weighted ? 2 : 0)) && h.src_size == size &&
+            h.flags == (uint32_t)((symmetric ? 1 : 0) | (weighted ? 2 : 0) | (dedup ? 4 : 0)) && h.src_size == size &&
             h.src_mtime_ns == mtime && h.rows == graph.rows && h.nnz >= 0 && h.nnz <= INT32_MAX;
   if (ok) {
     const int nnz = (int)h.nnz;
@@ -258,11 +273,11 @@ bool load_cache(const std::string& cpath, const std::string& input, DAWN::Graph:
 }
 
 void store_cache(const std::string& cpath, const std::string& input, const DAWN::Graph::Graph_t& graph,
-                 bool symmetric, bool weighted) {
+                 bool symmetric, bool weighted, bool dedup) {
   CacheHeader h = {};
   std::memcpy(h.magic, kCacheMagic, 8);
   h.version = 1;
-  h.flags = (symmetric ? 1 : 0) | (weighted ? 2 : 0);
+  h.flags = (symmetric ? 1 : 0) | (weighted ? 2 : 0) | (dedup ? 4 : 0);
   if (!source_stat(input, &h.src_size, &h.src_mtime_ns)) return;
   h.rows = graph.rows;
   h.nnz = (int64_t)graph.nnz;
@@ -282,16 +297,17 @@ void store_cache(const std::string& cpath, const std::string& input, const DAWN:
 }
 
 void read_any(std::string& input_path, DAWN::Graph::Graph_t& graph, bool symmetric, bool weighted) {
-  const std::string cpath = cache_path(input_path, symmetric, weighted);
-  if (!cpath.empty() && load_cache(cpath, input_path, graph, symmetric, weighted)) return;
+  const bool dedup = !weighted && dedup_requested();
+  const std::string cpath = cache_path(input_path, symmetric, weighted, dedup);
+  if (!cpath.empty() && load_cache(cpath, input_path, graph, symmetric, weighted, dedup)) return;
   std::string text;
   if (!read_all(input_path, &text)) {
     std::cerr << "Error opening file " << input_path << std::endl;
     return;
   }
   std::vector<Entry> e = parse_entries(text, weighted, graph.rows, input_path);
-  build(graph, e, symmetric, weighted);
-  if (!cpath.empty()) store_cache(cpath, input_path, graph, symmetric, weighted);
+  build(graph, e, symmetric, weighted, dedup);
+  if (!cpath.empty()) store_cache(cpath, input_path, graph, symmetric, weighted, dedup);
 }
 
 }  // namespace

@@ -146,3 +146,33 @@ def test_outfile_text_matches_printf(tmp_path):
     for ext, want in ((".is", want_is), (".fs", want_fs), (".i", want_i), (".f", want_f)):
         got = (tmp_path / ("out" + ext)).read_text()
         assert got == want, ext
+
+
+def test_dedup_option(goldens, tmp_path):
+    # DAWN_DEDUP=1 (opt-in, not in the reference): an unweighted read drops
+    # repeated (row, col) entries; a weighted read keeps them
+    env = dict(os.environ, DAWN_DEDUP="1")
+    for g in goldens:
+        out = str(tmp_path / "csr.bin")
+        r = subprocess.run([os.path.join(BIN_DIR, "dump_csr"), g.mtx, str(int(g.weighted)), "0", out],
+                           stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, env=env)
+        assert r.returncode == 0, r.stdout
+        with open(out, "rb") as f:
+            rows, _ = np.frombuffer(f.read(8), np.int32)
+            nnz = int(np.frombuffer(f.read(8), np.int64)[0])
+            f.read(8)
+            rp = np.frombuffer(f.read(4 * (rows + 1)), np.int32)
+            col = np.frombuffer(f.read(4 * nnz), np.int32)
+        if g.weighted:
+            assert np.array_equal(rp, g.row_ptr) and np.array_equal(col, g.col), g.name
+            continue
+        # the golden CSR (duplicates kept, rows sorted) with repeats removed
+        deg = np.diff(g.row_ptr.astype(np.int64))
+        row = np.repeat(np.arange(g.n), deg)
+        keep = np.ones(len(g.col), bool)
+        keep[1:] = (row[1:] != row[:-1]) | (g.col[1:] != g.col[:-1])
+        want_rp = np.concatenate([[0], np.cumsum(np.bincount(row[keep], minlength=g.n))])
+        assert np.array_equal(rp, want_rp), g.name
+        assert np.array_equal(col, g.col[keep]), g.name
+        if g.name.startswith("dups"):
+            assert keep.sum() < len(g.col), g.name  # the fixture does hold repeats
