@@ -7,17 +7,27 @@ int32 distances (nsrc x n) written to HBM.  The graph and sources are
 seeded synthetic data with the benchmark's shapes.
 
   value      whole-job GTEPS of the batched bitset traversal (CSR already
-             resident, distances left on the device), CUDA events on the
-             traversal stream around exactly --steps steps
+             resident, distances left on the device), DAWN_VARIANT_AUTO on
+             the autotuned handle (the learned selector runs when the tuner
+             measured it faster on this graph), CUDA events on the traversal
+             stream around exactly --steps steps
+  parity     the timed step's distances (and those of the heuristic and
+             single-source runs) against the reference CPU path's, bit for
+             bit; a mismatch exits non-zero
   e2e        the same metric through the C ABI with host buffers: per step
              dawn_graph_create from pinned host CSR + dawn_bfs into a pinned
              host array + dawn_graph_destroy
   plain      the same 64 sources through the single-source
-             direction-optimising kernels (for the batched-vs-plain ratio)
+             direction-optimising kernels, with its own roofline
+  selector   learned selector against the direction heuristic, median and
+             spread of repeated timings
   roofline   the dominant kernel's algorithmic bytes per launch / its
              CUDA-event launch time, from a traced replay of one step
-  cpu_baseline  the reference CPU path (MSSP_CPU::run restated, OpenMP over
-             sources, serial queue BFS each) on a bounded sample of sources
+  configs    the other benchmark configurations, one compact record each
+             (weighted RMAT-22, RMAT-18 x 4,096 sources, 512 ER graphs in
+             one launch), each with its parity flag against the oracle
+  cpu_baseline  the reference CPU path (MSSP_CPU::run: OpenMP over sources,
+             a serial queue BFS each) on all 64 sources, all host threads
 
 Multi-GPU: sources shard across ranks (each rank its own 64 sources on its
 own replica of the graph, no collective on the data path), weak scaling.
@@ -30,7 +40,6 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
 import time
 
 import numpy as np
@@ -42,6 +51,33 @@ SCALE, EDGEFACTOR, A, B, C = 22, 16, 0.57, 0.19, 0.19
 GRAPH_SEED, SOURCE_SEED, NSRC = 2022, 64, 64
 METRIC = "GTEPS per GB300 (BFS/SSSP/MSSP) learned+batched vs plain; % HBM roofline"
 L2_BYTES = 129 * 2 ** 20
+
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# headline step's kernels from one ncu capture, averaged over the launches of
+# one step.  Captured with:
+#   python bench.py --quick --traced --variant learned --steps 1 --warmup 1 &&
+#   ncu --nvtx --nvtx-include "dawn-step/" --clock-control none \
+#       --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum \
+#       --csv --log-file launches.csv python bench.py --quick --traced --variant learned --steps 1 --warmup 1
+# Keyed by kernel; a figure is reported only while the hash of the kernel's
+# source file matches the one it was captured on (None otherwise).
+NCU_TRAFFIC = {}
+
+
+def _source_hash(path):
+    import hashlib
+    try:
+        with open(os.path.join(ROOT, path), "rb") as f:
+            return hashlib.sha256(f.read()).hexdigest()[:16]
+    except OSError:
+        return None
+
+
+def ncu_traffic(kernel):
+    t = NCU_TRAFFIC.get(kernel)
+    if not t or _source_hash(t["file"]) != t["sha"]:
+        return None
+    return t
 
 
 def log(*a):
@@ -95,10 +131,11 @@ def peaks():
 
 
 class Clocks:
-    """nvidia-smi samples (every 50 ms) from the warm-up through the timed region."""
+    """nvidia-smi samples (every 50 ms) from the warm-up through the timed
+    region and the sustained window after it."""
     Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-         "clocks_event_reasons.sw_power_cap")
+         "clocks_event_reasons.sw_power_cap,utilization.gpu")
 
     def __init__(self, index):
         self.index = index
@@ -119,22 +156,26 @@ class Clocks:
         time.sleep(0.25)
         self.proc.terminate()
         out, _ = self.proc.communicate(timeout=10)
-        sm, mx, reasons = [], None, set()
+        sm, busy, mx, reasons = [], [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in out.strip().splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 6:
+            if len(f) < 7:
                 continue
             try:
                 sm.append(float(f[0]))
                 mx = float(f[1])
+                util = float(f[6])
             except ValueError:
                 continue
+            if util >= 50:
+                busy.append(sm[-1])
             for name, v in zip(names, f[2:6]):
                 if v.lower() == "active":
                     reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        load = busy or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm), "samples_under_load": len(busy)}
 
 
 def time_steps(torch, fn, steps, warmup, barrier):
@@ -153,113 +194,166 @@ def time_steps(torch, fn, steps, warmup, barrier):
     return e0.elapsed_time(e1)
 
 
-def HEADLINE_VARIANT(abi):
-    return abi.VARIANT_LEARNED
+def repeated(torch, fn, steps, reps):
+    """Median, lowest and highest ms per step over `reps` timings of `steps`
+    steps each."""
+    per = [time_steps(torch, fn, steps, 1, lambda: None) / steps for _ in range(reps)]
+    return statistics.median(per), min(per), max(per)
 
 
-def bitset_roofline(dg, g, srcs, d_dist, abi, peak_gbs, peak_kind):
-    """Traced replay of one step: per-kernel CUDA-event durations, and the
-    algorithmic bytes of each launch of the dominant kernel."""
-    dg.trace(True)
-    dg.bfs_device(srcs, d_dist, variant=HEADLINE_VARIANT(abi), stats=False)
-    dg.synchronize()
-    recs = dg.trace_read()
-    dg.trace(False)
-    for r in recs:
-        log("[trace] run %d level %d mode %d %-16s frontier %9d fedges %11d unfinished_edges %11d  %.3f ms" % (
-            r["run"], r["level"], r["mode"], r["kernel"], r["frontier"], r["frontier_edges"],
-            r["unvisited_edges"], r["ms"]))
+def alg_bytes(r, n, m):
+    """Algorithmic HBM bytes of one kernel launch in the unit of the
+    benchmark's roofline: CSR row pointers and columns read, distances
+    written; visited, frontier and level words count zero (they are
+    L2-sized at these graphs).
+
+    bs_pull / bfs_pull (one bottom-up sweep): row_ptr 4(n+1) and the
+      columns of the unfinished rows 4*mu.
+    bs_push_scatter / bfs_push: row_ptr + col of the frontier rows 4*(nf + mf).
+    bs_emit_dist: the 64 x n distance block written once.
+    """
+    k = r["kernel"]
+    if k in ("bs_pull", "bfs_pull"):
+        return 4 * (n + 1) + 4 * r["unvisited_edges"]
+    if k in ("bs_push_scatter", "bfs_push"):
+        return 4 * (r["frontier"] + r["frontier_edges"])
+    if k == "bs_emit_dist":
+        return 4 * NSRC * n
+    return 0
+
+
+def alg_bytes_with_words(r, n, m):
+    """The same, counting the bitset words each kernel must touch too (the
+    pull reads every unfinished vertex's visited words and writes its
+    frontier words: 16 bytes per vertex at one word per state)."""
+    k = r["kernel"]
+    if k == "bs_pull":
+        return alg_bytes(r, n, m) + 16 * n
+    if k == "bs_push_update":
+        return 24 * min(r["frontier_edges"], n)
+    if k == "bs_emit_dist":
+        return alg_bytes(r, n, m) + 40 * n
+    if k == "bs_clear":
+        return 8 * n * 9
+    if k == "bfs_pull":
+        return alg_bytes(r, n, m) + n // 8
+    return alg_bytes(r, n, m)
+
+
+def kernel_roofline(recs, n, m, peak_gbs, peak_kind, skip=("bs_init", "bs_next")):
+    """Per-kernel CUDA-event durations of a traced replay; the dominant
+    kernel's algorithmic bytes per launch over its average launch time."""
     per = {}
     for r in recs:
-        if r["kernel"] in ("bs_init", "bs_next"):  # one-thread bookkeeping
+        if r["kernel"] in skip:  # one-thread bookkeeping
             continue
-        k = per.setdefault(r["kernel"], {"launches": 0, "ms": 0.0, "bytes": 0})
+        k = per.setdefault(r["kernel"], {"launches": 0, "ms": 0.0, "bytes": 0, "bytes_w": 0})
         k["launches"] += 1
         k["ms"] += r["ms"]
-        k["bytes"] += alg_bytes(r, g.n, g.m)
+        k["bytes"] += alg_bytes(r, n, m)
+        k["bytes_w"] += alg_bytes_with_words(r, n, m)
+    if not per:
+        return None
     total = sum(k["ms"] for k in per.values())
     dom = max(per, key=lambda k: per[k]["ms"])
     k = per[dom]
     avg_ms = k["ms"] / k["launches"]
     avg_bytes = k["bytes"] / k["launches"]
     achieved = avg_bytes / (avg_ms * 1e-3) / 1e9
-    share = {name: round(v["ms"] / total, 4) for name, v in per.items()}
-    traffic = profiled_traffic(dom, int(round(np.log2(g.n))))
+    achieved_w = k["bytes_w"] / k["launches"] / (avg_ms * 1e-3) / 1e9
+    traffic = ncu_traffic(dom)
     return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak_gbs,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
-            "traffic": int(traffic) if traffic else None,
-            "traffic_source": "profiles/learned_bfs_rmat22_kernels.md (ncu dram__bytes_read.sum + "
-                              "dram__bytes_write.sum, per launch)" if traffic else None,
+            "traffic": int(traffic["bytes"]) if traffic else None,
+            "traffic_source": traffic["source"] if traffic else "not captured for this build",
             "launches_per_step": k["launches"], "avg_launch_ms": round(avg_ms, 4),
-            "alg_bytes_per_launch": int(avg_bytes), "kernel_share": share,
-            "source": "CUDA events around each kernel in a traced replay of one step"}, recs
+            "alg_bytes_per_launch": int(avg_bytes),
+            "alg_bytes_rule": "CSR row pointers and columns read + distances written; bitset words 0",
+            "with_bitset_words": {"achieved": round(achieved_w, 1), "frac": round(achieved_w / peak_gbs, 4),
+                                  "alg_bytes_per_launch": int(k["bytes_w"] / k["launches"])},
+            "kernel_share": {name: round(v["ms"] / total, 4) for name, v in per.items()},
+            "source": "CUDA events around each kernel in a traced replay"}
 
 
-def profiled_traffic(kernel, scale):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary of
-    this workload (profiles/learned_bfs_rmat22_kernels.md), or None."""
-    import re
-    p = os.path.join(ROOT, "profiles", "learned_bfs_rmat22_kernels.md")
-    if scale != 22 or not os.path.exists(p):
-        return None
-    m = re.search(kernel + r" DRAM traffic per launch, averaged over the step's \d+ launches: ([0-9.]+) MB",
-                  open(p).read())
-    return float(m.group(1)) * 1e6 if m else None
+def traced(dg, run):
+    dg.trace(True)
+    run()
+    dg.synchronize()
+    recs = dg.trace_read()
+    dg.trace(False)
+    return recs
 
 
-def alg_bytes(r, n, m):
-    """Algorithmic HBM bytes of one kernel launch (bitset traversal, 64 sources).
+def reached_edges(d_api, deg):
+    """TEPS numerator of a distance block: per source, the CSR entries whose
+    tail is reached (source row included)."""
+    return sum(int(deg[row >= 0].sum()) for row in d_api)
 
-    bs_pull (one level sweep): row_ptr 4(n+1), visited words read 8n,
-      frontier words written 8n, col of the unfinished rows 4*mu.
-    bs_push_scatter: row_ptr + col of the frontier rows 4*(nf + mf).
-    bs_push_update:  visited/next/frontier words of the touched vertices, bounded by 24*mf.
-    Distance writes (4 bytes per newly reached pair) are added per level by
-    the kernel that finds them; they are not visible in a level record and
-    are counted once per step in the step-level figure instead.
-    """
-    k = r["kernel"]
-    if k == "bs_pull":
-        return 4 * (n + 1) + 16 * n + 4 * r["unvisited_edges"]
-    if k == "bs_push_scatter":
-        return 4 * (r["frontier"] + r["frontier_edges"])
-    if k == "bs_push_update":
-        return 24 * min(r["frontier_edges"], n)
-    if k == "bs_emit_dist":
-        return 4 * NSRC * n + 8 * n * 5  # distance block written once + visited and level words read
-    if k == "bs_clear":
-        return 8 * n * 9  # visited, three frontier, next and four level words zeroed
-    if k == "bfs_pull":
-        return 4 * (n + 1) + n // 8 + 4 * r["unvisited_edges"]
-    if k == "bfs_push":
-        return 4 * (r["frontier"] + r["frontier_edges"])
-    return 0
+
+class _StdoutToStderr:
+    """The reference's CPU tools print progress lines ("Start print") to
+    stdout when they produce distances; they go to stderr here, so stdout
+    carries only the JSON line."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.saved = os.dup(1)
+        os.dup2(2, 1)
+
+    def __exit__(self, *exc):
+        try:
+            import ctypes
+            ctypes.CDLL(None).fflush(None)
+        except OSError:
+            pass
+        os.dup2(self.saved, 1)
+        os.close(self.saved)
 
 
 def _cpu_impl():
     """The reference CPU path: compiled from the reference's own sources when
-    that build loads here, else the oracle's restatement of it."""
+    that build loads here, else the oracle's restatement of it.  `run`
+    returns the distance block in the reference's encoding."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     threads = os.cpu_count() or 1
     if O.ref_available():
-        return O, "reference", threads, lambda g, s: O.ref_mssp(g, s, want_dist=False)
-    return O, "port", threads, lambda g, s: O.mssp(g, s, threads=threads, want_dist=False)
+        return O, "reference", threads, lambda g, s, want=True: O.ref_mssp(g, s, want_dist=want)[0]
+    return O, "port", threads, lambda g, s, want=True: O.mssp(g, s, threads=threads, want_dist=want)[0]
 
 
-def cpu_baseline(g, srcs):
+def cpu_baseline(g, srcs, edges):
     """All sources once through MSSP_CPU::run (OpenMP over sources, one
-    serial queue BFS each), wall-clock timed."""
+    serial queue BFS each), wall-clock timed; its distances are the parity
+    reference of the timed GPU step."""
     O, kind, threads, run = _cpu_impl()
-    edges = O.mssp(g, srcs[:1], threads=1, want_dist=False)[1]  # loads the port
-    edges = O.mssp(g, srcs, threads=threads, want_dist=False)[1] if kind == "reference" else None
-    t0 = time.perf_counter()
-    out = run(g, srcs)
-    dt = time.perf_counter() - t0
-    if edges is None:
-        edges = out[1]
+    O.mssp(g, srcs[:1], threads=1, want_dist=False)  # loads the library, warms the CSR pages
+    with _StdoutToStderr():
+        t0 = time.perf_counter()
+        ref = run(g, srcs)
+        dt = time.perf_counter() - t0
+    want = O.hops_ref_to_api(ref, srcs)
     return {"value": round(edges / dt / 1e9, 4), "unit": "GTEPS", "cores": threads, "kind": kind,
-            "sample": f"all {len(srcs)} sources once ({dt:.1f} s wall, {threads} threads)"}
+            "sample": f"all {len(srcs)} sources once ({dt:.1f} s wall, {threads} threads)",
+            "call": "MSSP_CPU::run (src/algorithm/cpu/mssp.cpp:9-32)"}, want
+
+
+def cpu_baseline_weighted(g, srcs):
+    """SSSP_CPU::SSSP per source (src/algorithm/cpu/sssp.cpp:23-80), one
+    source per thread on all host threads (the reference's own OpenMP
+    relax loses updates with more than one thread per source); the result
+    is the weighted parity reference."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    want = O.msssp(g, srcs, threads=threads)
+    dt = time.perf_counter() - t0
+    deg = g.degrees()
+    edges = sum(int(deg[row != np.float32(3.4028235e38)].sum()) for row in want)
+    return {"value": round(edges / dt / 1e9, 4), "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": f"all {len(srcs)} sources once ({dt:.1f} s wall, {threads} threads, one source per thread)",
+            "call": "SSSP_CPU::SSSP per source"}, want, edges
 
 
 def run_reference_arm(args):
@@ -268,21 +362,23 @@ def run_reference_arm(args):
         return
     g, srcs = make_workload(args.scale, 0)
     O, kind, threads, run = _cpu_impl()
-    # Per step: one wave of sources (one per thread), fewer when --steps is
-    # large, so the whole run stays within about three minutes.
-    one = time.perf_counter()
-    O.mssp(g, srcs[:1], threads=1, want_dist=False)
-    one = time.perf_counter() - one
-    per_step = max(1, min(len(srcs), threads))
-    if (args.steps + args.warmup) * one > 180:
-        per_step = 1
+    # One untimed pass over all sources gives the TEPS numerator and the
+    # time of a full step; a step covers every source unless the whole run
+    # would pass about four minutes, then the first sources only.
+    with _StdoutToStderr():
+        t0 = time.perf_counter()
+        want = O.hops_ref_to_api(run(g, srcs), srcs)
+        full = time.perf_counter() - t0
+    per_step = len(srcs)
+    while per_step > 1 and (args.steps + args.warmup) * full * per_step / len(srcs) > 240:
+        per_step //= 2
     sample = srcs[:per_step]
-    edges = O.mssp(g, sample, threads=threads, want_dist=False)[1]
+    edges = reached_edges(want[:per_step], g.degrees())
     for _ in range(args.warmup):
-        run(g, sample)
+        run(g, sample, False)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        run(g, sample)
+        run(g, sample, False)
     dt = time.perf_counter() - t0
     gteps = edges * args.steps / dt / 1e9
     line = {"impl": "reference", "metric": METRIC, "value": round(gteps, 4), "unit": "GTEPS", "n_gpus": ws,
@@ -460,6 +556,146 @@ def quick_multi(args, torch, abi, rank):
                           "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2)}), flush=True)
 
 
+def config_records(torch, abi, gen, stream, rank, g_w, srcs, peak_gbs, want_cpu):
+    """Compact records of the other benchmark configurations, each with its
+    parity flag against the oracle (rank 0 checks; other ranks report
+    None):
+
+      weighted   the headline topology with int32 and float32 weights in
+                 [1, 63]: 64 sources batched (min-plus, 64 per traversal)
+                 and single-source; SSSP_CPU::SSSP per source as baseline
+      rmat18x4096  RMAT-18, 4,096 sources, 256 per traversal (W = 4) on the
+                 autotuned handle; plain = single-source on the first 256
+      er512      512 directed ER graphs (n in [1,024, 65,536], average degree
+                 in [4, 32], 8-64 sources each) in one persistent launch;
+                 plain = single-source per graph on the first 32 graphs
+    """
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    threads = os.cpu_count() or 1
+    out = {}
+
+    def timed(fn, steps):
+        fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    # --- weighted, RMAT-22 topology x 64 sources -----------------------------
+    t_cfg = time.perf_counter()
+    want = cpu = None
+    if want_cpu:
+        cpu, want_np, _ = cpu_baseline_weighted(g_w, srcs)
+        want = torch.from_numpy(want_np).cuda()
+        del want_np
+    rec = {"workload": f"rmat22-ef16-sssp-{len(srcs)}src, weights int32 and float32 in [1,63]", "cpu_baseline": cpu}
+    eq = True
+    for w in ("i32", "f32"):
+        with abi.Graph(g_w, weights=w, stream=stream) as dg:
+            dt = torch.float32 if w == "f32" else torch.int32
+            d = torch.empty((len(srcs), g_w.n), dtype=dt, device="cuda")
+            st = dg.sssp_device(srcs, d.data_ptr(), variant=abi.VARIANT_AUTO)
+            ms_b = timed(lambda: dg.sssp_device(srcs, d.data_ptr(), stats=False, variant=abi.VARIANT_AUTO), 3)
+            if want is not None:
+                eq &= bool(torch.equal(_weighted_ref(torch, d, abi), want))
+            ms_s = timed(lambda: dg.sssp_device(srcs, d.data_ptr(), stats=False, variant=abi.VARIANT_DO), 1)
+            if want is not None:
+                eq &= bool(torch.equal(_weighted_ref(torch, d, abi), want))
+            e = st.edges_traversed
+            rec[w] = {"batched": {"ms_per_step": round(ms_b, 3), "gteps": round(e / (ms_b * 1e-3) / 1e9, 2),
+                                  "levels": st.levels},
+                      "plain": {"ms_per_step": round(ms_s, 3), "gteps": round(e / (ms_s * 1e-3) / 1e9, 2)},
+                      "speedup_vs_plain": round(ms_s / ms_b, 3)}
+            del d
+    rec["parity"] = {"equal": eq if want is not None else None, "sources": len(srcs),
+                     "against": "SSSP_CPU::SSSP per source (oracle)", "checked": ["batched", "single-source"]}
+    rec["wall_s"] = round(time.perf_counter() - t_cfg, 1)
+    out["weighted"] = rec
+    del want
+
+    # --- RMAT-18, 4,096 sources -------------------------------------------------
+    t_cfg = time.perf_counter()
+    g = gen.rmat(18, EDGEFACTOR, A, B, C, seed=GRAPH_SEED)
+    s4 = gen.sources(g, 4096, seed=SOURCE_SEED)
+    with abi.Graph(g, stream=stream) as dg:
+        tuning = dg.autotune(s4)
+        d = torch.empty((4096, g.n), dtype=torch.int32, device="cuda")
+        st = dg.bfs_device(s4, d.data_ptr(), variant=abi.VARIANT_AUTO)
+        ms_b = timed(lambda: dg.bfs_device(s4, d.data_ptr(), variant=abi.VARIANT_AUTO, stats=False), 3)
+        eq = None
+        k = 512
+        if want_cpu:
+            ref, _, _ = O.mssp(g, s4[:k], threads=threads)
+            eq = bool(torch.equal(d[:k], torch.from_numpy(O.hops_ref_to_api(ref, s4[:k])).cuda()))
+        e = st.edges_traversed
+        st2 = dg.bfs_device(s4[:256], d.data_ptr(), variant=abi.VARIANT_DO)
+        ms_p = timed(lambda: dg.bfs_device(s4[:256], d.data_ptr(), variant=abi.VARIANT_DO, stats=False), 1)
+        g_b, g_p = e / (ms_b * 1e-3) / 1e9, st2.edges_traversed / (ms_p * 1e-3) / 1e9
+        out["rmat18x4096"] = {"workload": "rmat18-ef16-bfs-4096src", "n": g.n, "m": g.m,
+                              "batched": {"ms_per_step": round(ms_b, 3), "gteps": round(g_b, 2),
+                                          "width": tuning["bitset_width"], "learned": tuning["learned"]},
+                              "plain": {"ms_per_256_sources": round(ms_p, 3), "gteps": round(g_p, 2)},
+                              "speedup_vs_plain": round(g_b / g_p, 3),
+                              "parity": {"equal": eq, "sources": k, "against": "MSSP_CPU::run (oracle)"},
+                              "wall_s": round(time.perf_counter() - t_cfg, 1)}
+        del d
+    del g
+
+    # --- 512 ER graphs, one persistent launch ------------------------------------
+    t_cfg = time.perf_counter()
+    graphs, gsrcs = gen.er_family(ngraphs=512, seed=GRAPH_SEED)
+    u, off = gen.disjoint_union(graphs)
+    with abi.Graph(u, stream=stream) as dg:
+        dg.set_parts(off)
+        d = torch.empty(dg.multi_out_size(gsrcs), dtype=torch.int32, device="cuda")
+        st = dg.multi_bfs_ptr(gsrcs, d.data_ptr(), device=True)
+        ms_b = timed(lambda: dg.multi_bfs_ptr(gsrcs, d.data_ptr(), device=True, stats=False), 5)
+        eq = None
+        if want_cpu:
+            eq = True
+            pos = 0
+            for g1, s1 in zip(graphs, gsrcs):
+                size = len(s1) * g1.n
+                ref, _, _ = O.mssp(g1, s1, threads=threads)
+                want = torch.from_numpy(O.hops_ref_to_api(ref, s1).reshape(-1)).cuda()
+                eq &= bool(torch.equal(d[pos:pos + size], want))
+                pos += size
+        e = st.edges_traversed
+        del d
+    sub = 32
+    ms_p, e_p = 0.0, 0
+    for g1, s1 in zip(graphs[:sub], gsrcs[:sub]):
+        with abi.Graph(g1, stream=stream) as dg:
+            d = torch.empty((len(s1), g1.n), dtype=torch.int32, device="cuda")
+            st1 = dg.bfs_device(s1, d.data_ptr(), variant=abi.VARIANT_DO)
+            ms_p += timed(lambda: dg.bfs_device(s1, d.data_ptr(), variant=abi.VARIANT_DO, stats=False), 1)
+            e_p += st1.edges_traversed
+    g_b, g_p = e / (ms_b * 1e-3) / 1e9, e_p / (ms_p * 1e-3) / 1e9
+    out["er512"] = {"workload": "512 directed ER graphs, 8-64 sources each, one persistent launch",
+                    "graphs": len(graphs), "sources": int(sum(len(x) for x in gsrcs)),
+                    "batched": {"ms_per_step": round(ms_b, 3), "gteps": round(g_b, 2)},
+                    "plain": {"graphs": sub, "ms": round(ms_p, 3), "gteps": round(g_p, 2)},
+                    "speedup_vs_plain": round(g_b / g_p, 3),
+                    "parity": {"equal": eq, "parts": len(graphs), "against": "MSSP_CPU::run per graph (oracle)"},
+                    "wall_s": round(time.perf_counter() - t_cfg, 1)}
+    return out
+
+
+def _weighted_ref(torch, d, abi):
+    """Device distances in the reference's float encoding (FLT_MAX for
+    unreachable)."""
+    if d.dtype == torch.float32:
+        return d
+    f = d.to(torch.float32)
+    return torch.where(d == abi.INT32_MAX, torch.tensor(float(abi.FLT_MAX), device=d.device), f)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -467,9 +703,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="dawn", choices=["dawn", "reference"])
     ap.add_argument("--scale", type=int, default=SCALE)
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and parity legs")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' records")
     ap.add_argument("--plain-steps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--reps", type=int, default=5, help="repeats of the selector-vs-heuristic timing")
+    ap.add_argument("--sustain-s", type=float, default=1.5,
+                    help="seconds of the headline step run after the timed region for the clock record")
     ap.add_argument("--quick", action="store_true",
                     help="only the device-resident timing (profiling runs); prints a short JSON line")
     ap.add_argument("--traced", action="store_true",
@@ -514,7 +754,8 @@ def main():
         else:
             srcs = _gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
     else:
-        g, srcs = make_workload(args.scale, rank, weighted=args.quick and args.variant.startswith("sssp"))
+        # weights drawn too: the weighted configuration shares the topology
+        g, srcs = make_workload(args.scale, rank, weighted=not args.quick or args.variant.startswith("sssp"))
     if args.quick:
         srcs = srcs[:args.sources]
     # A dedicated stream: the library launches on it and torch's events
@@ -563,51 +804,89 @@ def main():
                               "kernels": len(recs)}), flush=True)
         dg.close()
         return
-    # learned + batched: the bitset traversal with each level's variant picked
-    # by the trained selector (the library's default weights); the autotuner
-    # sets the handle's speed options first (untimed, once per graph)
+
+    # The reference CPU path first: its distances are the parity reference
+    # of every GPU run below (rank 0; other ranks wait at the barrier).
+    st0 = dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=True)
+    edges = st0.edges_traversed
+    cpu, want = None, None
+    if rank == 0 and not args.no_cpu:
+        cpu, want_np = cpu_baseline(g, srcs, edges)
+        want = torch.from_numpy(want_np).cuda()
+        del want_np
+    checks = {}
+
+    def check(name):
+        if want is not None:
+            torch.cuda.synchronize()
+            checks[name] = bool(torch.equal(d_dist, want))
+
+    check("untuned bitset")
+    # learned + batched: the autotuner sets the handle's speed options first
+    # (untimed, once per graph); AUTO then runs the batched traversal with the
+    # learned selector when the tuner measured it faster, else the heuristic
     tuning = None
     if not args.no_tune:
         tuning = dg.autotune(srcs)
-    var = HEADLINE_VARIANT(abi)
+    var = abi.VARIANT_AUTO
     step = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=False)  # noqa
     st = dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=True)
-    edges = st.edges_traversed
 
     clocks = Clocks(local)
     clocks.start()
     ms = time_steps(torch, step, args.steps, args.warmup, barrier)
+    check("headline (timed step)")
+    # a sustained window of the same step right after, so the clock record
+    # covers more than the short timed region
+    n_sus = max(args.steps, int(args.sustain_s * 1e3 / max(ms / args.steps, 1e-3)))
+    ms_sus = time_steps(torch, step, n_sus, 0, barrier) / n_sus
     clk = clocks.stop()
     # the slowest rank's time, the edges of all ranks
     ms_step, _, value = aggregate(torch, ms / args.steps, edges, ws, "cuda")
 
+    # learned selector against the direction heuristic, repeated
+    sel = {}
+    for name, v in (("learned", abi.VARIANT_LEARNED), ("heuristic", abi.VARIANT_BITSET)):
+        fn = lambda v=v: dg.bfs_device(srcs, d_dist.data_ptr(), variant=v, stats=False)  # noqa: E731
+        med, lo, hi = repeated(torch, fn, args.steps, args.reps)
+        check(f"batched {name}")
+        sel[name] = {"ms_median": round(med, 4), "ms_min": round(lo, 4), "ms_max": round(hi, 4),
+                     "gteps_median": round(edges / (med * 1e-3) / 1e9, 2)}
+    spread = max(sel["learned"]["ms_max"] - sel["learned"]["ms_min"],
+                 sel["heuristic"]["ms_max"] - sel["heuristic"]["ms_min"])
+    sel["learned_gain"] = round(sel["heuristic"]["ms_median"] / sel["learned"]["ms_median"] - 1.0, 4)
+    sel["beats_heuristic_beyond_spread"] = sel["heuristic"]["ms_median"] - sel["learned"]["ms_median"] > spread
+    sel["reps"] = args.reps
+    sel["auto_uses_selector"] = bool(tuning["learned"]) if tuning else False
+
     # plain single-source direction-optimising kernels, same sources
     step_plain = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_DO, stats=False)  # noqa
     ms_plain = time_steps(torch, step_plain, args.plain_steps, 1, barrier) / args.plain_steps
+    check("plain single-source")
+    reached = int((d_dist >= 0).sum().item())
+    plain_bytes = 4 * edges + 4 * (reached + NSRC) + 4 * g.n * NSRC
+    plain_ach = plain_bytes / (ms_plain * 1e-3) / 1e9
     plain = {"value": round(edges / (ms_plain * 1e-3) / 1e9, 3), "unit": "GTEPS",
-             "ms_per_step": round(ms_plain, 3), "variant": "single-source push/pull (direction-optimising)"}
-    # the same batched traversal under the direction heuristic alone
-    step_h = lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=False)  # noqa
-    ms_h = time_steps(torch, step_h, args.steps, args.warmup, barrier) / args.steps
-    st_h = dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=True)
-    batched_heuristic = {"value": round(edges / (ms_h * 1e-3) / 1e9, 3), "unit": "GTEPS",
-                         "ms_per_step": round(ms_h, 4), "push_levels": st_h.push_levels,
-                         "pull_levels": st_h.pull_levels,
-                         "variant": "batched bitset, direction heuristic (no selector)"}
+             "ms_per_step": round(ms_plain, 3), "variant": "single-source push/pull (direction-optimising)",
+             "roofline": {"bound": "hbm", "achieved": round(plain_ach, 1), "peak": peak_gbs, "peak_kind": peak_kind,
+                          "unit": "GB/s", "frac": round(plain_ach / peak_gbs, 4), "alg_bytes_per_step": plain_bytes,
+                          "alg_bytes_rule": "per source 4*m_r + 4*(n_r + 1) + 4*n (reached edges, reached "
+                                            "vertices, distance row)"}}
+    recs_plain = traced(dg, lambda: dg.bfs_device(srcs[:2], d_dist.data_ptr(), variant=abi.VARIANT_DO, stats=False))
+    plain["roofline"]["kernel"] = kernel_roofline(recs_plain, g.n, g.m, peak_gbs, peak_kind,
+                                                  skip=("bfs_init", "bfs_decide", "bs_init", "bs_next"))
 
-    if os.environ.get("DAWN_BENCH_TRACE_PLAIN"):
-        dg.trace(True)
-        dg.bfs_device(srcs[:2], d_dist.data_ptr(), variant=abi.VARIANT_DO, stats=False)
-        dg.synchronize()
-        for r in dg.trace_read():
-            log("[trace-plain] src %d level %d mode %d %-10s frontier %9d fedges %11d unvisited_edges %11d %.3f ms"
-                % (r["run"], r["level"], r["mode"], r["kernel"], r["frontier"], r["frontier_edges"],
-                   r["unvisited_edges"], r["ms"]))
-        dg.trace(False)
-    roof, recs = bitset_roofline(dg, g, srcs, d_dist.data_ptr(), abi, peak_gbs, peak_kind)
+    recs = traced(dg, lambda: dg.bfs_device(srcs, d_dist.data_ptr(), variant=var, stats=False))
+    check("traced replay")
+    for r in recs:
+        log("[trace] run %d level %d mode %d %-16s frontier %9d fedges %11d unfinished_edges %11d  %.3f ms" % (
+            r["run"], r["level"], r["mode"], r["kernel"], r["frontier"], r["frontier_edges"],
+            r["unvisited_edges"], r["ms"]))
+    roof = kernel_roofline(recs, g.n, g.m, peak_gbs, peak_kind)
     step_bytes = 4 * g.m + 4 * (g.n + 1) + NSRC * 4 * g.n
     roof["step_alg_bytes"] = step_bytes
     roof["step_achieved"] = round(step_bytes / (ms_step * 1e-3) / 1e9, 1)
+    roof["step_frac"] = round(step_bytes / (ms_step * 1e-3) / 1e9 / peak_gbs, 4)
 
     # end to end through the C ABI with pinned host buffers
     rp_h = torch.from_numpy(g.row_ptr).pin_memory()
@@ -634,6 +913,8 @@ def main():
 
     e2e_step()
     torch.cuda.synchronize()
+    if want is not None:
+        checks["e2e (host buffers)"] = bool(torch.equal(out_h, want.cpu()))
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         e2e_step(record=True)
@@ -646,30 +927,47 @@ def main():
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
            "phases_ms": {k: round(v / args.e2e_steps, 3) for k, v in phases.items()},
            "call": "dawn_graph_create(pinned host CSR) + dawn_bfs(pinned host dist) + dawn_graph_destroy"}
+    del want
+    dg.close()
+    del d_dist
 
-    cpu = None
-    if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(g, srcs)
+    configs = None
+    if not args.no_configs:
+        from dawn_gb300 import gen as _gen
+        configs = config_records(torch, abi, _gen, stream, rank, g, srcs, peak_gbs,
+                                 want_cpu=rank == 0 and not args.no_cpu)
 
-    launches = sum(1 for r in recs) + 3  # level kernels + clear/init/next per batch (traced count)
+    parity = None
+    if checks:
+        parity = {"config": f"rmat{args.scale} x {NSRC} sources", "equal": all(checks.values()),
+                  "sources": NSRC, "against": cpu["kind"] + " MSSP_CPU::run", "checked": checks}
+    launches = len(recs) + 3  # level kernels + clear/init/next per batch (traced count)
     line = {"metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
-            "config": {"workload": f"rmat{args.scale}-ef{EDGEFACTOR}-bfs-{NSRC}src-learned-bitset", "n": g.n,
+            "config": {"workload": f"rmat{args.scale}-ef{EDGEFACTOR}-bfs-{NSRC}src-batched-auto", "n": g.n,
                        "m": g.m,
                        "sources": NSRC, "edges_traversed_per_step": edges,
                        "l2": "inputs larger than L2 (CSR %.0f MB, distances %.0f MB per step)" % (
                            (4 * g.m + 4 * g.n) / 2 ** 20, 4 * NSRC * g.n / 2 ** 20),
                        "parallelism": f"sources sharded, {ws} replica(s)"},
-            "clocks": clk, "e2e": e2e, "plain": plain, "batched_heuristic": batched_heuristic, "tuning": tuning,
+            "parity": parity, "clocks": clk,
+            "sustained": {"steps": n_sus, "ms_per_step": round(ms_sus, 4),
+                          "value": round(edges / (ms_sus * 1e-3) / 1e9, 3)},
+            "e2e": e2e, "plain": plain, "selector": sel, "tuning": tuning,
             "speedup_vs_plain": round(value / plain["value"], 3) if plain["value"] else None,
-            "roofline": roof, "cpu_baseline": cpu, "gpu_launches": launches * args.steps,
+            "roofline": roof, "cpu_baseline": cpu, "configs": configs, "gpu_launches": launches * args.steps,
             "levels_per_step": st.levels, "push_levels": st.push_levels, "pull_levels": st.pull_levels}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    dg.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+    bad = [k for k, v in checks.items() if not v]
+    if configs:
+        bad += [k for k, v in configs.items() if v.get("parity", {}).get("equal") is False]
+    if bad:
+        log("[bench] PARITY MISMATCH: " + ", ".join(bad))
+        sys.exit(3)
 
 
 if __name__ == "__main__":

@@ -2,7 +2,7 @@
 //
 // The reference runs multi-source and all-pairs BFS as a serial loop of
 // single-source traversals (src/algorithm/gpu/mssp.cu:26-43,
-// src/algorithm/gpu/apsp.cu:183-200), re-reading the whole CSR once per
+// src/algorithm/gpu/apsp.cu:81-100), re-reading the whole CSR once per
 // source.  Here up to 64*W sources share one traversal: every vertex carries
 // W uint64 words per state (visited, frontier, next), bit b of word i
 // standing for source 64*i + b of the batch, so one pass over an adjacency

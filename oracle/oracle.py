@@ -22,12 +22,52 @@ _F = ctypes.POINTER(ctypes.c_float)
 _U8 = ctypes.POINTER(ctypes.c_uint8)
 
 
-def build(ref_dir="/root/reference", with_ref=None):
-    """Compile the restatement (and the reference when its sources exist)."""
+# The reference's source tree: $DAWN_REFERENCE_DIR, by default the read-only
+# checkout at /root/reference.  Machines without it (the GPU hosts) use the
+# install copy that stage_reference() leaves, untracked, under baseline/_ref/.
+REF_DEFAULT = "/root/reference"
+STAGED = os.path.join(os.path.dirname(HERE), "baseline", "_ref", "GAL-DAWN")
+STAGE_PARTS = ("src", "include", "algorithm", "LICENSE")
+
+
+def _has_src(d):
+    return bool(d) and os.path.isdir(os.path.join(d, "src", "algorithm", "cpu"))
+
+
+def reference_dir():
+    """The reference sources to compile from, or None."""
+    d = os.environ.get("DAWN_REFERENCE_DIR", REF_DEFAULT)
+    if _has_src(d):
+        return d
+    return STAGED if _has_src(STAGED) else None
+
+
+def stage_reference(ref_dir):
+    """Install copy of the unmodified reference sources under baseline/_ref/
+    (git-ignored, carried to GPU hosts with the working tree), so the
+    reference's own CPU path can be compiled on a machine that has no
+    checkout of it.  Nothing under it is ever edited."""
+    import shutil
+    if os.path.realpath(ref_dir) == os.path.realpath(STAGED):
+        return
+    os.makedirs(STAGED, exist_ok=True)
+    for part in STAGE_PARTS:
+        src, dst = os.path.join(ref_dir, part), os.path.join(STAGED, part)
+        if os.path.isdir(src):
+            shutil.copytree(src, dst, dirs_exist_ok=True)
+        elif os.path.exists(src):
+            shutil.copy2(src, dst)
+
+
+def build(ref_dir=None, with_ref=None):
+    """Compile the restatement, and the reference wherever its sources are
+    found (the checkout, or the staged install copy)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    ref_dir = ref_dir or reference_dir()
     if with_ref is None:
-        with_ref = os.path.isdir(os.path.join(ref_dir, "src"))
+        with_ref = _has_src(ref_dir)
     if with_ref:
+        stage_reference(ref_dir)
         subprocess.run(["make", "-s", "-C", HERE, "-j8", "ref", f"REF={ref_dir}"], check=True)
 
 

@@ -95,7 +95,7 @@ def parse_weighted(text, n, source):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("DAWN_REFERENCE_DIR", "/root/reference"))
     args = ap.parse_args()
     import oracle as O
     from dawn_gb300 import gen

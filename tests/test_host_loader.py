@@ -9,9 +9,10 @@ import subprocess
 import numpy as np
 import pytest
 
+import oracle as O
 from dawn_gb300 import BIN_DIR, HOST_DIR, INCLUDE_DIR, LIB_DIR, gen
 
-REF = "/root/reference"
+REF = O.reference_dir() or ""
 
 
 def dump(path, weighted, source, tmp):

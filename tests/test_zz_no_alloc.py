@@ -1,11 +1,13 @@
 """dawn_bfs_static, the entry point that allocates nothing (its working
-memory is one static block of device memory per GPU), against dawn_bfs on a
-handle of the same CSR.  Distances are integers, so the tolerance is zero.
-Collected last so it also runs after every other GPU test in one process."""
+memory is one static block of device memory per GPU), against the oracle's
+MSSP_CPU::run and against dawn_bfs on a handle of the same CSR.  Distances
+are integers, so the tolerance is zero.  Collected last so it also runs
+after every other GPU test in one process."""
 
 import numpy as np
 import pytest
 
+import oracle as O
 from dawn_gb300 import abi, gen
 
 pytestmark = pytest.mark.gpu
@@ -31,8 +33,11 @@ def test_static_matches_handle_path(graph):
     else:
         g = gen.erdos_renyi(abi.STATIC_MAX_VERTICES, 1 << 23, seed=33)
     srcs = gen.sources(g, 2, seed=32)
+    ref, _, _ = O.mssp(g, srcs)
+    want = O.hops_ref_to_api(ref, srcs)
     with abi.Graph(g) as dg:
-        want, _ = dg.bfs(srcs, variant=abi.VARIANT_PUSH)
+        handle, _ = dg.bfs(srcs, variant=abi.VARIANT_PUSH)
+    assert np.array_equal(handle, want)
     rp, col = _device(g.row_ptr), _device(g.col)
     dist = torch.empty(g.n, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
@@ -44,6 +49,13 @@ def test_static_matches_handle_path(graph):
     # and again, without the CSR check
     got = _static(g, rp, col, srcs[0], dist, flags=abi.GRAPH_NO_VALIDATE)
     assert np.array_equal(got, want[0])
+    # a further call takes no device memory: the free figure does not move
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    got = _static(g, rp, col, srcs[1], dist)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert np.array_equal(got, want[1])
 
 
 def test_static_rejects_what_it_cannot_hold():
