@@ -595,8 +595,10 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
 // and every other word the traversal touches lives in `g_static_scratch`.
 //
 // The block holds a graph of at most kStaticMaxVertices vertices and
-// kStaticMaxEdges edges (about 12.5 MiB); every GPU on which the library is
-// loaded keeps it until the process exits.  There is one block per device,
+// kStaticMaxEdges edges (about 12.5 MiB).  It exists on a GPU once the
+// library's kernels are loaded there (with lazy module loading, at the
+// first launch of one of them on that device) and stays until the process
+// exits.  There is one block per device,
 // so calls that overlap on one device (from two host threads, or on two
 // streams) race on it: the caller serialises them.
 

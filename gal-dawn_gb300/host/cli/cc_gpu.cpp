@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // cc_gpu: the reference's command-line tool (algorithm/gpu/cc_gpu/cc_gpu.cu)
 // over the GB300 path.  The closeness line keeps the reference's value; set
 // DAWN_EXACT_CC=1 to print the exact float64 closeness instead.

@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // mssp_gpu: the reference's command-line tool (algorithm/gpu/mssp_gpu/mssp_gpu.cu)
 // over the GB300 path: same flags, console lines and output file.
 #include <dawn/algorithm/gpu/mssp.cuh>

@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // sssp_gpu: the reference's command-line tool (algorithm/gpu/sssp_gpu/sssp_gpu.cu)
 // over the GB300 path: same flags, console lines and output file.
 #include <dawn/algorithm/gpu/sssp.cuh>

@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // MatrixMarket header handling and reader dispatch (API and messages of
 // src/graph.cpp:9-77 in the reference project).
 #include <dawn/graph.hxx>

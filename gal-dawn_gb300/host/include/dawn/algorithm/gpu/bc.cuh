@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // Betweenness centrality on the GPU, API of include/dawn/algorithm/gpu/bc.cuh
 // in the reference project (declared there, with no implementation).
 #pragma once

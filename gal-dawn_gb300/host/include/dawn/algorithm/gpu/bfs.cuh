@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // Single-source BFS on the GPU, API of include/dawn/algorithm/gpu/bfs.cuh
 // in the reference project (the reference's thrust-based kernel() helper is
 // internal and not part of this API).

@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // Closeness centrality on the GPU, API of include/dawn/algorithm/gpu/cc.cuh
 // in the reference project.
 #pragma once

@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // Standard headers the DAWN API and its command-line tools rely on.
 #pragma once
 #include <cfloat>

@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // File input/output, API of include/dawn/io.hxx in the reference project.
 #pragma once
 #include <dawn/graph.hxx>

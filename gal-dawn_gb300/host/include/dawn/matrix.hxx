@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // CSR / COO containers and conversions, API of include/dawn/matrix.hxx in
 // the reference project.
 #pragma once

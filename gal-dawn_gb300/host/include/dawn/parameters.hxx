@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // Command-line options, API of include/dawn/parameters.hxx in the reference
 // project (getopt flags -i -o -l -p -w -s -h).
 #pragma once

@@ -257,6 +257,10 @@ bool load_cache(const std::string& cpath, const std::string& input, DAWN::Graph:
          std::fread(col, sizeof(int), (size_t)nnz, f) == (size_t)nnz &&
          (!weighted || std::fread(val, sizeof(float), (size_t)nnz, f) == (size_t)nnz) && rp[0] == 0 &&
          rp[graph.rows] == nnz;
+    // A damaged cache must not reach the GPU unchecked (the device-side CSR
+    // check can be switched off): rows never shrink, columns in [0, rows).
+    for (int v = 0; ok && v < graph.rows; v++) ok = rp[v] <= rp[v + 1];
+    for (int k = 0; ok && k < nnz; k++) ok = col[k] >= 0 && col[k] < graph.rows;
     if (ok) {
       graph.nnz = (uint64_t)nnz;
       graph.csr.row_ptr = rp;

@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // Command-line parsing (flags, messages and exit codes of
 // src/parameters.cpp:3-98 in the reference project).
 #include <dawn/parameters.hxx>

@@ -1,3 +1,5 @@
+// Derived from GAL-DAWN (lxrzlyr/GAL-DAWN), Copyright (c) 2024 lxrzlyr,
+// Apache License 2.0 (see NOTICE): interface kept for drop-in use.
 // Progress and averaging helpers (API of src/tool.cpp in the reference).
 #include <dawn/tool.hxx>
 

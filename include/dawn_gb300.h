@@ -127,8 +127,8 @@ dawn_status dawn_bfs_device(dawn_graph* g, const int32_t* sources,
  *   CSR check that otherwise runs first.  stream orders the work (NULL: the
  *   default stream); the call returns once the traversal has finished.
  * Working memory is one fixed block of device memory per GPU, declared by
- * the library (about 12.5 MiB, held on every GPU where the library is
- * loaded until the process exits), so a graph is limited to
+ * the library (about 12.5 MiB, held on each GPU once the library's
+ * kernels are loaded there, until the process exits), so a graph is limited to
  * DAWN_STATIC_MAX_VERTICES vertices and DAWN_STATIC_MAX_EDGES edges; larger
  * ones are rejected with DAWN_ERR_INVALID_ARG.  The first call on a device
  * looks up that device's block; make it before any stream capture.  Calls

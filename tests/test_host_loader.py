@@ -116,6 +116,20 @@ def test_csr_cache(goldens, tmp_path):
             f.truncate(40)
         _, t4 = load()
         assert t4 != t3 and path.stat().st_size > 40
+        # damaged contents under an intact header: a column outside [0, n),
+        # then a row pointer that decreases; each is parsed again (load()
+        # checks the CSR equals the fixture's) and the cache rewritten
+        header, t = 48, t4
+        if g.m == 0:
+            continue
+        for offset, value in ((header + 4 * (g.n + 1), g.n), (header + 4, g.row_ptr[1] + g.m + 1)):
+            with open(path, "r+b") as f:
+                f.seek(offset)
+                f.write(np.array([value], np.int32).tobytes())
+            time.sleep(0.01)
+            _, t_new = load()
+            assert t_new != t, (g.name, offset)
+            t = t_new
 
 
 def test_outfile_text_matches_printf(tmp_path):
