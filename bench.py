@@ -322,10 +322,13 @@ def _cpu_impl():
     return O, "port", threads, lambda g, s, want=True: O.mssp(g, s, threads=threads, want_dist=want)[0]
 
 
-def cpu_baseline(g, srcs, edges):
+def cpu_baseline(g, srcs):
     """All sources once through MSSP_CPU::run (OpenMP over sources, one
     serial queue BFS each), wall-clock timed; its distances are the parity
-    reference of the timed GPU step."""
+    reference of the timed GPU step.  Runs before the process creates its
+    CUDA context: on the Grace host, first touches of fresh host pages (the
+    reference allocates three n-sized arrays per source) cost several times
+    more in a process that holds one."""
     O, kind, threads, run = _cpu_impl()
     O.mssp(g, srcs[:1], threads=1, want_dist=False)  # loads the library, warms the CSR pages
     with _StdoutToStderr():
@@ -333,6 +336,7 @@ def cpu_baseline(g, srcs, edges):
         ref = run(g, srcs)
         dt = time.perf_counter() - t0
     want = O.hops_ref_to_api(ref, srcs)
+    edges = reached_edges(want, g.degrees())
     return {"value": round(edges / dt / 1e9, 4), "unit": "GTEPS", "cores": threads, "kind": kind,
             "sample": f"all {len(srcs)} sources once ({dt:.1f} s wall, {threads} threads)",
             "call": "MSSP_CPU::run (src/algorithm/cpu/mssp.cpp:9-32)"}, want
@@ -556,7 +560,7 @@ def quick_multi(args, torch, abi, rank):
                           "gteps": round(st.edges_traversed / (ms * 1e-3) / 1e9, 2)}), flush=True)
 
 
-def config_records(torch, abi, gen, stream, rank, g_w, srcs, peak_gbs, want_cpu):
+def config_records(torch, abi, gen, stream, rank, g_w, srcs, peak_gbs, want_cpu, weighted_ref=None):
     """Compact records of the other benchmark configurations, each with its
     parity flag against the oracle (rank 0 checks; other ranks report
     None):
@@ -591,7 +595,7 @@ def config_records(torch, abi, gen, stream, rank, g_w, srcs, peak_gbs, want_cpu)
     t_cfg = time.perf_counter()
     want = cpu = None
     if want_cpu:
-        cpu, want_np, _ = cpu_baseline_weighted(g_w, srcs)
+        cpu, want_np = weighted_ref if weighted_ref else cpu_baseline_weighted(g_w, srcs)[:2]
         want = torch.from_numpy(want_np).cuda()
         del want_np
     rec = {"workload": f"rmat22-ef16-sssp-{len(srcs)}src, weights int32 and float32 in [1,63]", "cpu_baseline": cpu}
@@ -728,9 +732,21 @@ def main():
     if args.impl == "reference":
         return run_reference_arm(args)
 
+    ws, rank, local = dist_env()
+    # The reference CPU path first, before this process creates a CUDA
+    # context: its distances are the parity reference of every GPU run
+    # below (rank 0; other ranks meet it at the process-group set-up).
+    g = srcs = None
+    cpu = want_np = weighted_ref = None
+    if not args.quick:
+        # weights drawn too: the weighted configuration shares the topology
+        g, srcs = make_workload(args.scale, rank, weighted=True)
+        if rank == 0 and not args.no_cpu:
+            cpu, want_np = cpu_baseline(g, srcs)
+            if not args.no_configs:
+                weighted_ref = cpu_baseline_weighted(g, srcs)[:2]
     import torch
     from dawn_gb300 import abi
-    ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     barrier = lambda: None  # noqa: E731
     if ws > 1:
@@ -753,9 +769,8 @@ def main():
             srcs = _gen.sources(g, NSRC, seed=2, from_lcc=False)
         else:
             srcs = _gen.sources(g, NSRC, seed=SOURCE_SEED + rank)
-    else:
-        # weights drawn too: the weighted configuration shares the topology
-        g, srcs = make_workload(args.scale, rank, weighted=not args.quick or args.variant.startswith("sssp"))
+    elif args.quick:
+        g, srcs = make_workload(args.scale, rank, weighted=args.variant.startswith("sssp"))
     if args.quick:
         srcs = srcs[:args.sources]
     # A dedicated stream: the library launches on it and torch's events
@@ -805,13 +820,10 @@ def main():
         dg.close()
         return
 
-    # The reference CPU path first: its distances are the parity reference
-    # of every GPU run below (rank 0; other ranks wait at the barrier).
     st0 = dg.bfs_device(srcs, d_dist.data_ptr(), variant=abi.VARIANT_BITSET, stats=True)
     edges = st0.edges_traversed
-    cpu, want = None, None
-    if rank == 0 and not args.no_cpu:
-        cpu, want_np = cpu_baseline(g, srcs, edges)
+    want = None
+    if want_np is not None:
         want = torch.from_numpy(want_np).cuda()
         del want_np
     checks = {}
@@ -935,7 +947,8 @@ def main():
     if not args.no_configs:
         from dawn_gb300 import gen as _gen
         configs = config_records(torch, abi, _gen, stream, rank, g, srcs, peak_gbs,
-                                 want_cpu=rank == 0 and not args.no_cpu)
+                                 want_cpu=rank == 0 and not args.no_cpu, weighted_ref=weighted_ref)
+        weighted_ref = None
 
     parity = None
     if checks:

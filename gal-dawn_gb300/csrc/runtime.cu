@@ -149,7 +149,7 @@ dawn_status add_kernel(cudaGraph_t graph, cudaGraphNode_t* node, const cudaGraph
   p.func = const_cast<void*>(l.fn);
   p.gridDim = l.grid;
   p.blockDim = l.block;
-  p.sharedMemBytes = 0;
+  p.sharedMemBytes = (unsigned)l.smem;
   p.kernelParams = l.args;
   p.extra = nullptr;
   DAWN_CUDA(cudaGraphAddKernelNode(node, graph, dep, dep ? 1 : 0, &p));
@@ -223,7 +223,7 @@ dawn_status build_graph(SsFamily& fam, cudaGraphExec_t* exec) {
 
 dawn_status launch(const Launch& l, cudaStream_t s, const cudaAccessPolicyWindow* w = nullptr) {
   if (!w) {
-    DAWN_CUDA(cudaLaunchKernel(l.fn, l.grid, l.block, l.args, 0, s));
+    DAWN_CUDA(cudaLaunchKernel(l.fn, l.grid, l.block, l.args, l.smem, s));
     return DAWN_OK;
   }
   cudaLaunchAttribute attr;
@@ -232,7 +232,7 @@ dawn_status launch(const Launch& l, cudaStream_t s, const cudaAccessPolicyWindow
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = l.grid;
   cfg.blockDim = l.block;
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = l.smem;
   cfg.stream = s;
   cfg.attrs = &attr;
   cfg.numAttrs = 1;
