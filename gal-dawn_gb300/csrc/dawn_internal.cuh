@@ -213,14 +213,6 @@ struct dawn_graph {
   dawn::DevBuf hv_segoff;       // exclusive prefix of their segment counts (nh + 1)
   dawn::DevBuf hv_acc;          // per heavy row: OR accumulator + finished-segment count
   int32_t hv_count = 0, hv_segs = 0;
-  // Hub table of the bitset pull: the hub_n tails that occur most often in
-  // the in-edge columns have their frontier words copied into each CTA's
-  // shared memory at the start of a pull level; hub_col is the in-edge
-  // column array with those tails written as ~(rank in hub_v).
-  dawn::DevBuf hub_col;         // int32[m + 8]
-  dawn::DevBuf hub_v;           // int32[hub_n], vertex of each rank
-  int32_t hub_n = 0;            // hubs the table holds (0: not built)
-  int32_t hub_w = 0;            // bitset width the table was built for
   int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges
   int32_t bs_width = 0;         // words per vertex of the bitset traversal (0 = by source count)
   int32_t force_variant = 0;    // 0 = decide per level, else 1 + variant for every level

@@ -89,21 +89,6 @@ static_assert(kDeepLevel == 1 << kShallowBits, "slices hold exactly the levels b
 // Heavy pull rows: a row of at least 2 x seg in-edges (seg = the handle's
 // pull segment, 1024 by default) is cut into seg-entry warp tasks.
 
-// Hub table of the pull.  The pull is bound by its random gathers of
-// in-neighbours' frontier words through L1/TEX and L2 (one per in-edge).
-// On power-law graphs a few tails carry a large share of the in-edges
-// (RMAT-22: the top 20,480 by out-degree are 43% of all in-edge entries),
-// so each CTA copies those tails' frontier words into shared memory at the
-// start of a pull level, and the in-edge columns name them by their rank
-// in the table (~rank, a negative number): their gathers become shared-
-// memory loads.  The table is loaded only when the level's unfinished
-// in-edges are worth it (at least kHubLoadFactor x CTAs x table entries).
-constexpr int kPullBlock = 1024;                 // threads per CTA of bs_pull
-constexpr size_t kHubBytes = (size_t)160 << 10;  // table bytes per CTA
-constexpr int kHubLoadFactor = 2;
-constexpr int32_t kNoCol = INT32_MIN;            // "no entry" in the gather loops
-__host__ __device__ constexpr int hub_capacity(int w) { return (int)(kHubBytes / (8 * (size_t)w)); }
-
 // Words per heavy-row accumulator: W bits and a finished-segment counter,
 // rounded up to an even count so the W words start 16-byte aligned for
 // the vectorised loads.
@@ -427,12 +412,9 @@ struct LevelAcc {
 // exit once no missing bit is left), shorter ones are walked by one lane
 // each.  The list is filtered into the next unfinished list as it goes.
 template <int W>
-__global__ void __launch_bounds__(kPullBlock, 1) bs_pull(const int32_t* __restrict__ row_ptr,
+__global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t* __restrict__ row_ptr,
                                                      const int32_t* __restrict__ t_row_ptr,
-                                                     const int32_t* __restrict__ t_col,
-                                                     const int32_t* __restrict__ hub_col,
-                                                     const int32_t* __restrict__ hub_v, int32_t hub_n,
-                                                     BsCtl* __restrict__ ctl,
+                                                     const int32_t* __restrict__ t_col, BsCtl* __restrict__ ctl,
                                                      u64* __restrict__ visit, u64* __restrict__ fr,
                                                      u64* __restrict__ slices, int32_t* __restrict__ aq,
                                                      Seg* __restrict__ segs, size_t segcap,
@@ -441,23 +423,11 @@ __global__ void __launch_bounds__(kPullBlock, 1) bs_pull(const int32_t* __restri
                                                      const int32_t* __restrict__ hv_segoff, u64* __restrict__ hv_acc,
                                                      int32_t hv_count, int32_t hv_segs, int32_t pull_seg, int32_t n) {
   using B = Bits<W>;
-  extern __shared__ __align__(16) u64 s_hub[];
-  __shared__ int32_t s_qa[kPullBlock / 32][kWarpQueueBig];
-  __shared__ int32_t s_qu[kPullBlock / 32][kWarpQueueBig];
+  __shared__ int32_t s_qa[kBlock / 32][kWarpQueueBig];
+  __shared__ int32_t s_qu[kBlock / 32][kWarpQueueBig];
   if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
   const u64* __restrict__ fin = fr + (size_t)((L - 1) % 3) * n * W;
-  // The frontier words of level L - 1 are read-only during this level, so
-  // every CTA's copy of the hubs' words stays exact for the whole launch.
-  const bool use_hub = hub_n > 0 && ctl->mu >= (long long)kHubLoadFactor * gridDim.x * hub_n;
-  const int32_t* __restrict__ tc = use_hub ? hub_col : t_col;
-  if (use_hub) {
-    for (int i = threadIdx.x; i < hub_n; i += blockDim.x)
-      B::ldg(fin + (size_t)__ldg(hub_v + i) * W).st(s_hub + (size_t)i * W);
-    __syncthreads();
-  }
-  // A column entry c >= 0 is a vertex; c < 0 is hub ~c of the table.
-  auto gather = [&](int32_t c) -> B { return c < 0 ? B::ld(s_hub + (size_t)(~c) * W) : B::ldg(fin + (size_t)c * W); };
   u64* __restrict__ fout = fr + (size_t)(L % 3) * n * W;
   int32_t* aq_out = aq + (size_t)(L % 3) * n;
   Seg* seg_out = segs + (size_t)(L % 3) * segcap;
@@ -500,14 +470,14 @@ __global__ void __launch_bounds__(kPullBlock, 1) bs_pull(const int32_t* __restri
     B w = B::zero();
     for (int k0 = ks; k0 < ke; k0 += 128) {
       const int k = k0 + lane;
-      const int32_t v0 = k < ke ? __ldg(tc + k) : kNoCol;
-      const int32_t v1 = k + 32 < ke ? __ldg(tc + k + 32) : kNoCol;
-      const int32_t v2 = k + 64 < ke ? __ldg(tc + k + 64) : kNoCol;
-      const int32_t v3 = k + 96 < ke ? __ldg(tc + k + 96) : kNoCol;
-      if (v0 != kNoCol) w = w | gather(v0);
-      if (v1 != kNoCol) w = w | gather(v1);
-      if (v2 != kNoCol) w = w | gather(v2);
-      if (v3 != kNoCol) w = w | gather(v3);
+      const int32_t v0 = k < ke ? __ldg(t_col + k) : -1;
+      const int32_t v1 = k + 32 < ke ? __ldg(t_col + k + 32) : -1;
+      const int32_t v2 = k + 64 < ke ? __ldg(t_col + k + 64) : -1;
+      const int32_t v3 = k + 96 < ke ? __ldg(t_col + k + 96) : -1;
+      if (v0 >= 0) w = w | B::ldg(fin + (size_t)v0 * W);
+      if (v1 >= 0) w = w | B::ldg(fin + (size_t)v1 * W);
+      if (v2 >= 0) w = w | B::ldg(fin + (size_t)v2 * W);
+      if (v3 >= 0) w = w | B::ldg(fin + (size_t)v3 * W);
       if ((w.warp_or() | vis | B::ldcg(hacc)) == full) break;
     }
     w = w.warp_or();
@@ -575,14 +545,14 @@ __global__ void __launch_bounds__(kPullBlock, 1) bs_pull(const int32_t* __restri
       B w = B::zero();
       for (int k0 = s; k0 < e; k0 += 128) {
         const int k = k0 + lane;
-        const int32_t v0 = k < e ? __ldg(tc + k) : kNoCol;
-        const int32_t v1 = k + 32 < e ? __ldg(tc + k + 32) : kNoCol;
-        const int32_t v2 = k + 64 < e ? __ldg(tc + k + 64) : kNoCol;
-        const int32_t v3 = k + 96 < e ? __ldg(tc + k + 96) : kNoCol;
-        if (v0 != kNoCol) w = w | gather(v0);
-        if (v1 != kNoCol) w = w | gather(v1);
-        if (v2 != kNoCol) w = w | gather(v2);
-        if (v3 != kNoCol) w = w | gather(v3);
+        const int32_t v0 = k < e ? __ldg(t_col + k) : -1;
+        const int32_t v1 = k + 32 < e ? __ldg(t_col + k + 32) : -1;
+        const int32_t v2 = k + 64 < e ? __ldg(t_col + k + 64) : -1;
+        const int32_t v3 = k + 96 < e ? __ldg(t_col + k + 96) : -1;
+        if (v0 >= 0) w = w | B::ldg(fin + (size_t)v0 * W);
+        if (v1 >= 0) w = w | B::ldg(fin + (size_t)v1 * W);
+        if (v2 >= 0) w = w | B::ldg(fin + (size_t)v2 * W);
+        if (v3 >= 0) w = w | B::ldg(fin + (size_t)v3 * W);
         if ((w.warp_or() | lvis) == full) break;
       }
       w = w.warp_or();
@@ -600,12 +570,12 @@ __global__ void __launch_bounds__(kPullBlock, 1) bs_pull(const int32_t* __restri
       // gathers instead of eight.
       B w = B::zero();
       for (int a = rs & ~7; a < re; a += 8) {
-        const int4 x = __ldg(reinterpret_cast<const int4*>(tc + a));
-        const int4 y = a + 4 < re ? __ldg(reinterpret_cast<const int4*>(tc + a + 4)) : make_int4(0, 0, 0, 0);
+        const int4 x = __ldg(reinterpret_cast<const int4*>(t_col + a));
+        const int4 y = a + 4 < re ? __ldg(reinterpret_cast<const int4*>(t_col + a + 4)) : make_int4(0, 0, 0, 0);
         const int32_t c[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
 #pragma unroll
         for (int j = 0; j < 8; j++)
-          if (a + j >= rs && a + j < re) w = w | gather(c[j]);
+          if (a + j >= rs && a + j < re) w = w | B::ldg(fin + (size_t)c[j] * W);
         if ((w | vis) == full) break;
       }
       got = w;
@@ -1103,83 +1073,7 @@ __global__ void scatter_flagged(const int64_t* __restrict__ flags, const int64_t
     }
 }
 
-__global__ void hub_ranks(const int32_t* __restrict__ hub_v, int32_t hub_n, int32_t* __restrict__ rank) {
-  const int stride = gridDim.x * blockDim.x;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < hub_n; i += stride) rank[hub_v[i]] = i;
-}
-
-// hub_col[k] = ~rank of t_col[k] when that tail is in the table, else t_col[k].
-// (A column outside [0, n), possible only when the caller skipped the CSR
-// check, is copied as it is.)
-__global__ void hub_encode(const int32_t* __restrict__ t_col, long long m, const int32_t* __restrict__ rank,
-                           int32_t n, int32_t* __restrict__ hub_col) {
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < (size_t)m; k += stride) {
-    const int32_t v = t_col[k];
-    const int32_t r = v >= 0 && v < n ? __ldg(rank + v) : -1;
-    hub_col[k] = r >= 0 ? ~r : v;
-  }
-}
-
 }  // namespace
-
-// Hub table of the bitset pull at width w: the hub_capacity(w) vertices of
-// largest out-degree (the tails that occur most often in the in-edge
-// columns; ties to the lower id), in id order, and the in-edge columns
-// re-encoded to name them by rank.  Both buffers are sized once for the
-// largest table (w = 1), so their addresses, which captured graphs hold,
-// never change.  Without room for the encoded columns the pull runs
-// without a table.
-dawn_status build_hub_table(dawn_graph* g, int w) {
-  const int32_t n = g->n;
-  const int32_t h = std::min<int64_t>(n, hub_capacity(w));
-  if (g->hub_w == w && g->hub_n == h) return DAWN_OK;
-  // captured traversal graphs hold the table's size as a launch argument
-  for (cudaGraphExec_t& e : g->bs_exec)
-    if (e) {
-      cudaGraphExecDestroy(e);
-      e = nullptr;
-    }
-  g->hub_n = 0;
-  g->hub_w = 0;
-  if (h == 0 || g->m == 0) return DAWN_OK;
-  std::vector<int32_t> rp((size_t)n + 1);
-  DAWN_CUDA(cudaMemcpyAsync(rp.data(), g->row_ptr, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyDeviceToHost,
-                            g->stream));
-  DAWN_CUDA(cudaStreamSynchronize(g->stream));
-  std::vector<int32_t> idx((size_t)n);
-  for (int32_t v = 0; v < n; v++) idx[v] = v;
-  auto more = [&](int32_t a, int32_t b) {
-    const int32_t da = rp[a + 1] - rp[a], db = rp[b + 1] - rp[b];
-    return da != db ? da > db : a < b;
-  };
-  if (h < n) std::nth_element(idx.begin(), idx.begin() + h, idx.end(), more);
-  idx.resize(h);
-  std::sort(idx.begin(), idx.end());
-  const int32_t cap = std::min<int64_t>(n, hub_capacity(1));
-  if (ensure(g->hub_v, sizeof(int32_t) * (size_t)cap, g->stream) != DAWN_OK ||
-      ensure(g->hub_col, sizeof(int32_t) * ((size_t)g->m + 8), g->stream) != DAWN_OK) {
-    clear_error();
-    release(g->hub_col);
-    return DAWN_OK;
-  }
-  DAWN_CUDA(cudaMemcpyAsync(g->hub_v.p, idx.data(), sizeof(int32_t) * (size_t)h, cudaMemcpyHostToDevice,
-                            g->stream));
-  int32_t* rank = nullptr;
-  DAWN_CHECK(pool_alloc((void**)&rank, sizeof(int32_t) * (size_t)n, g->stream));
-  DAWN_CUDA(cudaMemsetAsync(rank, 0xff, sizeof(int32_t) * (size_t)n, g->stream));
-  hub_ranks<<<g->geo.sms, kBlock, 0, g->stream>>>(g->hub_v.as<int32_t>(), h, rank);
-  DAWN_CUDA(cudaGetLastError());
-  // the spare entries past m are read (never used) by the aligned loads
-  DAWN_CUDA(cudaMemsetAsync(g->hub_col.as<int32_t>() + g->m, 0, sizeof(int32_t) * 8, g->stream));
-  hub_encode<<<g->geo.sms * 8, kBlock, 0, g->stream>>>(g->t_col, g->m, rank, n, g->hub_col.as<int32_t>());
-  DAWN_CUDA(cudaGetLastError());
-  pool_free(rank, g->stream);
-  DAWN_CUDA(cudaStreamSynchronize(g->stream));
-  g->hub_n = h;
-  g->hub_w = w;
-  return DAWN_OK;
-}
 
 // Static pull lists of the in-edge CSR (shared with the weighted pull).
 dawn_status build_static_list(dawn_graph* g) {
@@ -1246,7 +1140,6 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
       }
   }
   DAWN_CHECK(build_static_list(g));
-  DAWN_CHECK(build_hub_table(g, W));
   // words (per vertex W each): visit | fr[3] | nxt | level slices[nbits]
   // lists: aq[3] | tq | ul[2] | touched bitmap ; segments[3]
   // Levels never exceed n, and levels from kDeepLevel on bypass the slices.
@@ -1290,8 +1183,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
 
   struct {
     BsCtl* ctl;
-    const int32_t *row_ptr, *col, *t_row_ptr, *t_col, *ul_static, *hub_col, *hub_v;
-    int32_t hub_n;
+    const int32_t *row_ptr, *col, *t_row_ptr, *t_col, *ul_static;
     u64 *words, *visit, *fr, *fr0, *nxt, *slices;
     int32_t *aq, *aq0, *tq, *ul;
     uint32_t* tbm;
@@ -1313,9 +1205,6 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   a.col = g->col;
   a.t_row_ptr = g->t_row_ptr;
   a.t_col = g->t_col;
-  a.hub_col = g->hub_n > 0 ? g->hub_col.as<int32_t>() : nullptr;
-  a.hub_v = g->hub_n > 0 ? g->hub_v.as<int32_t>() : nullptr;
-  a.hub_n = g->hub_n;
   a.ul_static = g->ul_static.as<int32_t>();
   a.ul_static_size = g->ul_static_size;
   a.hv_static = g->hv_static.as<int32_t>();
@@ -1344,7 +1233,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   a.in_graph = 0;
   void* clear_args[] = {&a.words, &a.nwords};
   void* init_args[] = {&a.ctl, &a.row_ptr, &a.t_row_ptr, &a.visit, &a.fr0, &a.aq0, &a.segs, &a.n, &a.m};
-  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.hub_col, &a.hub_v, &a.hub_n, &a.ctl, &a.visit, &a.fr, &a.slices, &a.aq, &a.segs,
+  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.slices, &a.aq, &a.segs,
                        &a.segcap, &a.ul_static, &a.ul_static_size, &a.ul, &a.hv_static, &a.hv_segoff,
                        &a.hv_acc, &a.hv_count, &a.hv_segs, &a.pull_seg, &a.n};
   void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
@@ -1360,12 +1249,8 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   fam.pre[0] = {(const void*)bs_clear, clear_args, dim3(sms * 8), dim3(kBlock), "bs_clear"};
   fam.pre[1] = {(const void*)bs_init<W>, init_args, dim3(1), dim3(64 * W), "bs_init"};
   fam.nbody = 4;
-  const size_t hub_smem = sizeof(u64) * W * (size_t)g->hub_n;
-  DAWN_CUDA(cudaFuncSetAttribute((const void*)bs_pull<W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(sizeof(u64) * W * (size_t)hub_capacity(W))));
-  fam.body[0] = {(const void*)bs_pull<W>, pull_args,
-                 dim3(persistent_blocks((const void*)bs_pull<W>, kPullBlock, hub_smem, g->blocks_per_sm)),
-                 dim3(kPullBlock), "bs_pull", kModePull, hub_smem};
+  fam.body[0] = {(const void*)bs_pull<W>, pull_args, dim3(persistent_blocks((const void*)bs_pull<W>, kBlock, 0, g->blocks_per_sm)),
+                 dim3(kBlock), "bs_pull", kModePull};
   fam.body[1] = {(const void*)bs_push_scatter<W>, scatter_args,
                  dim3(persistent_blocks((const void*)bs_push_scatter<W>, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
                  "bs_push_scatter", kModePush};
