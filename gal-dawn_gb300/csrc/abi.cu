@@ -120,11 +120,11 @@ dawn_status start_graph(dawn_wtype wtype, int32_t n, int64_t m, uint32_t flags, 
     DAWN_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
     g->own_stream = true;
   }
-  // col / val carry 16 spare bytes so 128-bit loads at a row's end stay in bounds.
+  // col / val carry 32 spare bytes so 256-bit loads at a row's end stay in bounds.
   DAWN_CHECK(dawn::pool_alloc((void**)&g->row_ptr, sizeof(int32_t) * ((size_t)n + 1), g->stream));
-  DAWN_CHECK(dawn::pool_alloc((void**)&g->col, sizeof(int32_t) * (size_t)(m > 0 ? m : 1) + 16, g->stream));
+  DAWN_CHECK(dawn::pool_alloc((void**)&g->col, sizeof(int32_t) * (size_t)(m > 0 ? m : 1) + 32, g->stream));
   if (wtype != DAWN_W_NONE)
-    DAWN_CHECK(dawn::pool_alloc(&g->val, sizeof(int32_t) * (size_t)(m > 0 ? m : 1) + 16, g->stream));
+    DAWN_CHECK(dawn::pool_alloc(&g->val, sizeof(int32_t) * (size_t)(m > 0 ? m : 1) + 32, g->stream));
   return DAWN_OK;
 }
 

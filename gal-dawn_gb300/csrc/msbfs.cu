@@ -283,6 +283,51 @@ __device__ __forceinline__ void clear_next_slice(u64* __restrict__ slices, int32
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n * W; i += stride) p[i] = 0ull;
 }
 
+template <int W>
+__device__ __forceinline__ void clear_listed(u64* __restrict__ fr, const int32_t* __restrict__ list, int cnt,
+                                             const Seg* __restrict__ segs, int nsegs);
+
+// Column loads of the pull.  The in-edge columns stream through once per
+// level, so they bypass L1 and are marked first to leave L2 (the frontier
+// words they index are what L1 and L2 should keep).  A lane reads its short
+// row 32 bytes at a time: one sector per load where two 16-byte loads
+// cost two sector lookups in L1/TEX, whose sector throughput bounds the
+// pull (one sector per in-edge for the gather of its frontier word).
+__device__ __forceinline__ uint64_t evict_first_policy() {
+  uint64_t pol;
+  asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ int32_t ld_col(const int32_t* p, uint64_t pol) {
+  int32_t v;
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+  return v;
+}
+// p must be 32-byte aligned; the eight entries may run up to 28 bytes past
+// the row (the column arrays carry 32 spare bytes).
+__device__ __forceinline__ void ld_col8(const int32_t* p, uint64_t pol, int32_t (&c)[8]) {
+  asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+      : "=r"(c[0]), "=r"(c[1]), "=r"(c[2]), "=r"(c[3]), "=r"(c[4]), "=r"(c[5]), "=r"(c[6]), "=r"(c[7])
+      : "l"(p), "l"(pol));
+}
+
+// Zero the frontier words of a stale active list and its segment list
+// (grid-stride).  A list that covers more than a quarter of the vertices is
+// cleared as the whole slot instead: n coalesced word stores cost less than
+// that many scattered partial-sector writes.
+template <int W>
+__device__ __forceinline__ void clear_stale(u64* __restrict__ fr, int32_t n, const int32_t* __restrict__ list,
+                                            int cnt, const Seg* __restrict__ segs, int nsegs) {
+  if ((long long)cnt * 4 <= n) {
+    clear_listed<W>(fr, list, cnt, segs, nsegs);
+    return;
+  }
+  // 8-byte stores: a slot starts on an 8-byte boundary only (n * W words
+  // per slot, n odd possible), and a warp's 32 of them still fill two lines.
+  const size_t words = (size_t)n * W, stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < words; i += stride) fr[i] = 0ull;
+}
+
 // Zero the frontier words listed in a stale active list and its segment
 // list (grid-stride).
 template <int W>
@@ -433,8 +478,9 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
   Seg* seg_out = segs + (size_t)(L % 3) * segcap;
   int32_t* aq_count = &ctl->aq_size[L % 3];
   u64* al_pack = &ctl->alpack[L % 3];
-  clear_listed<W>(fr + (size_t)((L + 1) % 3) * n * W, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
-                  segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
+  clear_stale<W>(fr + (size_t)((L + 1) % 3) * n * W, n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
+                 segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
+  const uint64_t pol = evict_first_policy();
   clear_next_slice<W>(slices, n, L, ctl->nbits);
   const int cur = ctl->ul_cur;
   const int32_t* ul_in = cur < 0 ? ul_static : ul + (size_t)cur * n;
@@ -470,10 +516,10 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
     B w = B::zero();
     for (int k0 = ks; k0 < ke; k0 += 128) {
       const int k = k0 + lane;
-      const int32_t v0 = k < ke ? __ldg(t_col + k) : -1;
-      const int32_t v1 = k + 32 < ke ? __ldg(t_col + k + 32) : -1;
-      const int32_t v2 = k + 64 < ke ? __ldg(t_col + k + 64) : -1;
-      const int32_t v3 = k + 96 < ke ? __ldg(t_col + k + 96) : -1;
+      const int32_t v0 = k < ke ? ld_col(t_col + k, pol) : -1;
+      const int32_t v1 = k + 32 < ke ? ld_col(t_col + k + 32, pol) : -1;
+      const int32_t v2 = k + 64 < ke ? ld_col(t_col + k + 64, pol) : -1;
+      const int32_t v3 = k + 96 < ke ? ld_col(t_col + k + 96, pol) : -1;
       if (v0 >= 0) w = w | B::ldg(fin + (size_t)v0 * W);
       if (v1 >= 0) w = w | B::ldg(fin + (size_t)v1 * W);
       if (v2 >= 0) w = w | B::ldg(fin + (size_t)v2 * W);
@@ -545,10 +591,10 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
       B w = B::zero();
       for (int k0 = s; k0 < e; k0 += 128) {
         const int k = k0 + lane;
-        const int32_t v0 = k < e ? __ldg(t_col + k) : -1;
-        const int32_t v1 = k + 32 < e ? __ldg(t_col + k + 32) : -1;
-        const int32_t v2 = k + 64 < e ? __ldg(t_col + k + 64) : -1;
-        const int32_t v3 = k + 96 < e ? __ldg(t_col + k + 96) : -1;
+        const int32_t v0 = k < e ? ld_col(t_col + k, pol) : -1;
+        const int32_t v1 = k + 32 < e ? ld_col(t_col + k + 32, pol) : -1;
+        const int32_t v2 = k + 64 < e ? ld_col(t_col + k + 64, pol) : -1;
+        const int32_t v3 = k + 96 < e ? ld_col(t_col + k + 96, pol) : -1;
         if (v0 >= 0) w = w | B::ldg(fin + (size_t)v0 * W);
         if (v1 >= 0) w = w | B::ldg(fin + (size_t)v1 * W);
         if (v2 >= 0) w = w | B::ldg(fin + (size_t)v2 * W);
@@ -563,16 +609,14 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
     // memory and no search per edge: the L1/TEX path carries only the
     // column loads and the gathers.
     if (active && deg < kPullLaneMax) {
-      // The row is read in 32-byte aligned chunks of eight entries, two
-      // 16-byte loads each (the first from before the row start when it is
-      // not aligned; in-edge arrays carry 16 spare bytes, so neither load
-      // passes their end), so a lane issues two column loads per eight
-      // gathers instead of eight.
+      // The row is read in 32-byte aligned chunks of eight entries, one
+      // 32-byte load each (from before the row start when it is not
+      // aligned; in-edge arrays carry 32 spare bytes, so no load passes
+      // their end), so a lane issues one column load per eight gathers.
       B w = B::zero();
       for (int a = rs & ~7; a < re; a += 8) {
-        const int4 x = __ldg(reinterpret_cast<const int4*>(t_col + a));
-        const int4 y = a + 4 < re ? __ldg(reinterpret_cast<const int4*>(t_col + a + 4)) : make_int4(0, 0, 0, 0);
-        const int32_t c[8] = {x.x, x.y, x.z, x.w, y.x, y.y, y.z, y.w};
+        int32_t c[8];
+        ld_col8(t_col + a, pol, c);
 #pragma unroll
         for (int j = 0; j < 8; j++)
           if (a + j >= rs && a + j < re) w = w | B::ldg(fin + (size_t)c[j] * W);
@@ -628,8 +672,8 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
   const int qn = ctl->aq_size[(L - 1) % 3];
   const int ln = seg_count(ctl->alpack[(L - 1) % 3]);
   const bool dense = ctl->dense != 0;
-  clear_listed<W>(fr + (size_t)((L + 1) % 3) * n * W, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
-                  segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
+  clear_stale<W>(fr + (size_t)((L + 1) % 3) * n * W, n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
+                 segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
   clear_next_slice<W>(slices, n, L, ctl->nbits);
   const int wib = threadIdx.x >> 5;
   // The first two levels expand the sources and their neighbours, whose
@@ -1140,6 +1184,10 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
       }
   }
   DAWN_CHECK(build_static_list(g));
+  if (reinterpret_cast<uintptr_t>(g->t_col) % 32 != 0) {  // the pull's 256-bit column loads
+    set_error("in-edge column array is not 32-byte aligned");
+    return DAWN_ERR_CUDA;
+  }
   // words (per vertex W each): visit | fr[3] | nxt | level slices[nbits]
   // lists: aq[3] | tq | ul[2] | touched bitmap ; segments[3]
   // Levels never exceed n, and levels from kDeepLevel on bypass the slices.

@@ -556,7 +556,7 @@ dawn_status build_transpose(dawn_graph* g) {
   DAWN_CUDA(cudaGetLastError());
   DAWN_CHECK(exclusive_scan_i64(reinterpret_cast<const int64_t*>(deg), off, (int64_t)n + 1, s));
   DAWN_CHECK(pool_alloc((void**)&g->t_row_ptr, sizeof(int32_t) * ((size_t)n + 1), s));
-  DAWN_CHECK(pool_alloc((void**)&g->t_col, sizeof(int32_t) * (size_t)(g->m > 0 ? g->m : 1) + 16, s));
+  DAWN_CHECK(pool_alloc((void**)&g->t_col, sizeof(int32_t) * (size_t)(g->m > 0 ? g->m : 1) + 32, s));
   offsets_to_rowptr<<<grid, kBlock, 0, s>>>(off, g->t_row_ptr, deg, n);
   DAWN_CUDA(cudaGetLastError());
   scatter_in_edges<<<grid, kBlock, 0, s>>>(g->row_ptr, g->col, n, deg, g->t_col);
