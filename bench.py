@@ -810,6 +810,10 @@ def main():
         ms = time_steps(torch, quick, args.steps, 0, barrier) / max(1, args.steps)
         recs = dg.trace_read() if args.traced else []
         dg.trace(False)
+        for r in recs:
+            log("[trace] run %d level %d mode %d %-16s frontier %9d fedges %11d unfinished_edges %11d  %.3f ms" % (
+                r["run"], r["level"], r["mode"], r["kernel"], r["frontier"], r["frontier_edges"],
+                r["unvisited_edges"], r["ms"]))
         st = run(True)
         if rank == 0:
             print(json.dumps({"quick": True, "variant": args.variant, "traced": args.traced, "graph": args.graph,
@@ -885,6 +889,10 @@ def main():
                           "alg_bytes_rule": "per source 4*m_r + 4*(n_r + 1) + 4*n (reached edges, reached "
                                             "vertices, distance row)"}}
     recs_plain = traced(dg, lambda: dg.bfs_device(srcs[:2], d_dist.data_ptr(), variant=abi.VARIANT_DO, stats=False))
+    for r in recs_plain:
+        log("[trace-plain] src %d level %d mode %d %-10s frontier %9d fedges %11d unvisited_edges %11d %.3f ms"
+            % (r["run"], r["level"], r["mode"], r["kernel"], r["frontier"], r["frontier_edges"],
+               r["unvisited_edges"], r["ms"]))
     plain["roofline"]["kernel"] = kernel_roofline(recs_plain, g.n, g.m, peak_gbs, peak_kind,
                                                   skip=("bfs_init", "bfs_decide", "bs_init", "bs_next"))
 
