@@ -84,7 +84,8 @@ dawn_status finish_graph(dawn_graph* g, uint32_t flags) {
   } else {
     DAWN_CHECK(dawn::build_transpose(g));
   }
-  DAWN_CUDA(cudaMallocHost(&g->h_ctl, 2 * sizeof(dawn::SsCtl)));
+  static_assert(2 * sizeof(dawn::SsCtl) <= dawn::kPinnedSlot, "control-block copies exceed a pinned slot");
+  DAWN_CHECK(dawn::pinned_slot((void**)&g->h_ctl));
   DAWN_CHECK(dawn::ensure(g->sel_slot, sizeof(float) * DAWN_SELECTOR_WEIGHTS, g->stream));
   DAWN_CUDA(cudaEventCreate(&g->ev0));
   DAWN_CUDA(cudaEventCreate(&g->ev1));
@@ -150,8 +151,8 @@ void destroy(dawn_graph* g) {
     if (e) cudaGraphExecDestroy(e);
   if (g->pt_exec) cudaGraphExecDestroy(g->pt_exec);
   if (g->mw_exec) cudaGraphExecDestroy(g->mw_exec);
-  if (g->h_ctl) cudaFreeHost(g->h_ctl);
-  if (g->bc_h_level) cudaFreeHost(g->bc_h_level);
+  dawn::pinned_slot_release(g->h_ctl);
+  dawn::pinned_slot_release(g->bc_h_level);
   for (cudaEvent_t e : g->trace_ev)
     if (e) cudaEventDestroy(e);
   if (g->ev0) cudaEventDestroy(g->ev0);

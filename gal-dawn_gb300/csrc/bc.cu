@@ -320,7 +320,7 @@ dawn_status betweenness(dawn_graph* g, const int32_t* sources, int32_t nsrc, dou
   DAWN_CHECK(ensure(g->bc_terms, sizeof(float) * kLanes * nn, g->stream));
   DAWN_CHECK(ensure(g->bc_range, sizeof(int32_t) * 2 * nn * 2, g->stream));
   DAWN_CHECK(prepare_heavy(g));
-  if (!g->bc_h_level) DAWN_CUDA(cudaMallocHost(&g->bc_h_level, 2 * sizeof(int32_t)));
+  if (!g->bc_h_level) DAWN_CHECK(pinned_slot((void**)&g->bc_h_level));
   DAWN_CUDA(cudaMemsetAsync(d_bc, 0, sizeof(double) * nn, g->stream));
   int32_t* const Ls[2] = {g->bc_levels.as<int32_t>(), g->bc_levels.as<int32_t>() + kLanes * nn};
   int32_t* const Rs[2] = {g->bc_range.as<int32_t>(), g->bc_range.as<int32_t>() + 2 * nn};

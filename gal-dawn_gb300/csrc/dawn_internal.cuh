@@ -50,6 +50,14 @@ struct DevBuf {
 dawn_status ensure(DevBuf& b, size_t bytes, cudaStream_t s);
 void release(DevBuf& b);
 dawn_status pool_alloc(void** p, size_t bytes, cudaStream_t s);
+// Small page-locked host slots (up to kPinnedSlot bytes) for a handle's
+// control-block copies, carved from chunks that live until the process
+// exits: creating and destroying a handle then never calls cudaFreeHost,
+// which waits for the whole device, so handles on other streams keep
+// running while one is destroyed.
+constexpr size_t kPinnedSlot = 512;
+dawn_status pinned_slot(void** p);
+void pinned_slot_release(void* p);
 void pool_free(void* p, cudaStream_t s);
 
 // --- single-source frontier traversal (BOVM push/pull, GOVM push) ---------

@@ -46,6 +46,30 @@ void pool_free(void* p, cudaStream_t s) {
   if (p) cudaFreeAsync(p, s);
 }
 
+namespace {
+std::mutex g_pin_mu;
+std::vector<void*> g_pin_free;
+constexpr int kPinnedChunkSlots = 64;
+}  // namespace
+
+dawn_status pinned_slot(void** p) {
+  std::lock_guard<std::mutex> lock(g_pin_mu);
+  if (g_pin_free.empty()) {
+    char* chunk = nullptr;
+    DAWN_CUDA(cudaMallocHost((void**)&chunk, kPinnedSlot * kPinnedChunkSlots));
+    for (int i = kPinnedChunkSlots - 1; i >= 0; i--) g_pin_free.push_back(chunk + (size_t)i * kPinnedSlot);
+  }
+  *p = g_pin_free.back();
+  g_pin_free.pop_back();
+  return DAWN_OK;
+}
+
+void pinned_slot_release(void* p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lock(g_pin_mu);
+  g_pin_free.push_back(p);
+}
+
 dawn_status ensure(DevBuf& b, size_t bytes, cudaStream_t s) {
   if (bytes == 0) bytes = 16;
   if (b.bytes >= bytes) return DAWN_OK;
