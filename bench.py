@@ -330,7 +330,10 @@ def cpu_baseline(g, srcs):
     reference allocates three n-sized arrays per source) cost several times
     more in a process that holds one."""
     O, kind, threads, run = _cpu_impl()
-    O.mssp(g, srcs[:1], threads=1, want_dist=False)  # loads the library, warms the CSR pages
+    # loads the library and warms the CSR pages; OpenMP's thread count is
+    # process-wide state of the one runtime both libraries share, so this
+    # call also leaves it at all host threads for the reference's loop
+    O.mssp(g, srcs[:1], threads=threads, want_dist=False)
     with _StdoutToStderr():
         t0 = time.perf_counter()
         ref = run(g, srcs)
