@@ -310,6 +310,43 @@ class _StdoutToStderr:
         os.close(self.saved)
 
 
+def link_rates(torch, rp_h, col_h, out_h, d_dist):
+    """Copy-engine rates of the host link for the e2e step's own buffers:
+    the CSR in, the distance block out, and both at once on two streams
+    (best of three each)."""
+    d_rp = torch.empty(rp_h.shape, dtype=rp_h.dtype, device="cuda")
+    d_col = torch.empty(col_h.shape, dtype=col_h.dtype, device="cuda")
+    s0, s1 = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def timed(fn):
+        best = None
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t
+            best = dt if best is None else min(best, dt)
+        return best
+
+    def up():
+        d_rp.copy_(rp_h, non_blocking=True)
+        d_col.copy_(col_h, non_blocking=True)
+
+    def both():
+        with torch.cuda.stream(s0):
+            up()
+        with torch.cuda.stream(s1):
+            out_h.copy_(d_dist, non_blocking=True)
+
+    bi = rp_h.numel() * 4 + col_h.numel() * 4
+    bo = out_h.numel() * 4
+    t_in, t_out, t_both = timed(up), timed(lambda: out_h.copy_(d_dist, non_blocking=True)), timed(both)
+    del d_rp, d_col
+    return {"h2d_gbs": round(bi / t_in / 1e9, 1), "d2h_gbs": round(bo / t_out / 1e9, 1),
+            "both_ms": round(t_both * 1e3, 3), "in_then_out_ms": round((t_in + t_out) * 1e3, 3)}
+
+
 def _cpu_impl():
     """The reference CPU path: compiled from the reference's own sources when
     that build loads here, else the oracle's restatement of it.  `run`
@@ -911,25 +948,23 @@ def main():
     roof["step_achieved"] = round(step_bytes / (ms_step * 1e-3) / 1e9, 1)
     roof["step_frac"] = round(step_bytes / (ms_step * 1e-3) / 1e9 / peak_gbs, 4)
 
-    # end to end through the C ABI with pinned host buffers: one call at a
-    # time (sequential), then as a stream of calls with two in flight on
-    # two host threads and streams, so one call's CSR upload overlaps the
-    # other's distance download (the headline e2e)
+    # end to end through the C ABI with pinned host buffers, and the host
+    # link's own rates for the same bytes (a step moves the CSR in and the
+    # distance block out; the link carries one direction at a time here:
+    # both copies at once take as long as the two in turn)
     rp_h = torch.from_numpy(g.row_ptr).pin_memory()
     col_h = torch.from_numpy(g.col).pin_memory()
-    lanes = 2
-    out_h = [torch.empty((NSRC, g.n), dtype=torch.int32).pin_memory() for _ in range(lanes)]
-    e2e_streams = [stream] + [torch.cuda.Stream().cuda_stream for _ in range(lanes - 1)]
+    out_h = torch.empty((NSRC, g.n), dtype=torch.int32).pin_memory()
     phases = {"create_ms": 0.0, "bfs_ms": 0.0, "destroy_ms": 0.0}
 
-    def e2e_step(lane=0, record=False):
+    def e2e_step(record=False):
         t0 = time.perf_counter()
         h = abi.Graph(raw=dict(n=g.n, m=g.m, row_ptr=rp_h.data_ptr(), col=col_h.data_ptr(), symmetric=True,
-                               stream=e2e_streams[lane]))
+                               stream=stream))
         if tuning is not None:
             h.autotune(srcs, use_cache=True)  # the graph class's tuned settings, nothing measured
         t1 = time.perf_counter()
-        h.bfs_host_ptr(srcs, out_h[lane].data_ptr(), variant=var)
+        h.bfs_host_ptr(srcs, out_h.data_ptr(), variant=var)
         t2 = time.perf_counter()
         h.close()
         t3 = time.perf_counter()
@@ -938,56 +973,27 @@ def main():
             phases["bfs_ms"] += (t2 - t1) * 1e3
             phases["destroy_ms"] += (t3 - t2) * 1e3
 
-    for lane in range(lanes):
-        e2e_step(lane)
+    e2e_step()
     torch.cuda.synchronize()
     if want is not None:
-        want_h = want.cpu()
-        for lane in range(lanes):
-            checks[f"e2e (host buffers, stream {lane})"] = bool(torch.equal(out_h[lane], want_h))
-        del want_h
+        checks["e2e (host buffers)"] = bool(torch.equal(out_h, want.cpu()))
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        e2e_step(0, record=True)
+        e2e_step(record=True)
     torch.cuda.synchronize()
-    seq_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
-    seq_ms, _, seq_gteps = aggregate(torch, seq_ms, edges, ws, "cuda")
-
-    import threading
-    errors = []
-
-    def worker(lane, count):
-        try:
-            torch.cuda.set_device(local)
-            for _ in range(count):
-                e2e_step(lane)
-        except Exception as exc:  # reported after the join
-            errors.append(exc)
-
-    total = args.e2e_steps * lanes
-    threads = [threading.Thread(target=worker, args=(lane, total // lanes)) for lane in range(lanes)]
-    barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for t in threads:
-        t.start()
-    for t in threads:
-        t.join()
-    torch.cuda.synchronize()
-    pipe_ms = (time.perf_counter() - t0) * 1e3 / total
-    if errors:
-        raise errors[0]
-    pipe_ms, _, pipe_gteps = aggregate(torch, pipe_ms, edges, ws, "cuda")
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.e2e_steps
+    e2e_ms, _, e2e_gteps = aggregate(torch, e2e_ms, edges, ws, "cuda")
     h2d = 4 * (g.n + 1) + 4 * g.m + 4 * NSRC
     d2h = 4 * NSRC * g.n
-    call = "dawn_graph_create(pinned host CSR) + dawn_bfs(pinned host dist) + dawn_graph_destroy"
-    e2e = {"value": round(pipe_gteps, 3), "unit": "GTEPS", "ms_per_step": round(pipe_ms, 3),
-           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "in_flight": lanes, "steps": total,
-           "call": call + f", {lanes} calls in flight (host threads, one stream each)",
-           "sequential": {"value": round(seq_gteps, 3), "unit": "GTEPS", "ms_per_step": round(seq_ms, 3),
-                          "steps": args.e2e_steps,
-                          "phases_ms": {k: round(v / args.e2e_steps, 3) for k, v in phases.items()},
-                          "call": call + ", one call at a time"}}
+    link = link_rates(torch, rp_h, col_h, out_h, d_dist)
+    bound_ms = h2d / (link["h2d_gbs"] * 1e6) + d2h / (link["d2h_gbs"] * 1e6) + ms_step
+    e2e = {"value": round(e2e_gteps, 3), "unit": "GTEPS", "ms_per_step": round(e2e_ms, 3),
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+           "phases_ms": {k: round(v / args.e2e_steps, 3) for k, v in phases.items()},
+           "call": "dawn_graph_create(pinned host CSR) + dawn_bfs(pinned host dist) + dawn_graph_destroy",
+           "link": link, "bound_ms": round(bound_ms, 3), "frac_of_bound": round(bound_ms / e2e_ms, 4),
+           "bound_rule": "CSR in at the measured host-to-device rate + distances out at the measured "
+                         "device-to-host rate + the device-resident step"}
     del want
     dg.close()
     del d_dist

@@ -24,41 +24,21 @@ void set_error(const char* fmt, ...) {
 void clear_error() { g_err[0] = 0; }
 const char* last_error() { return g_err; }
 
-// Device memory comes from one stream-ordered pool per device owned by the
-// library (the device's default pool and its settings stay the
-// application's).  The pool keeps what it has (no release threshold), and
-// a block freed on one stream is not handed to an allocation on another
-// stream behind an implicit wait for that free: handles working on
-// different streams (calls in flight at once) would otherwise queue behind
-// each other's destroys.  Memory freed on a stream is reused at once on
-// that same stream, and across streams once the free has completed.
 namespace {
 std::once_flag g_pool_once[64];
-cudaMemPool_t g_pool[64] = {};
-cudaError_t g_pool_err[64] = {};
 }
 
 dawn_status pool_alloc(void** p, size_t bytes, cudaStream_t s) {
   int dev = 0;
   DAWN_CUDA(cudaGetDevice(&dev));
   std::call_once(g_pool_once[dev & 63], [dev]() {
-    cudaMemPoolProps props = {};
-    props.allocType = cudaMemAllocationTypePinned;
-    props.location.type = cudaMemLocationTypeDevice;
-    props.location.id = dev;
-    cudaMemPool_t pool = nullptr;
-    cudaError_t e = cudaMemPoolCreate(&pool, &props);
-    if (e == cudaSuccess) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
       uint64_t keep = UINT64_MAX;
-      int no = 0;
       cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
-      cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
-      g_pool[dev & 63] = pool;
     }
-    g_pool_err[dev & 63] = e;
   });
-  DAWN_CUDA(g_pool_err[dev & 63]);
-  DAWN_CUDA(cudaMallocFromPoolAsync(p, bytes ? bytes : 16, g_pool[dev & 63], s));
+  DAWN_CUDA(cudaMallocAsync(p, bytes ? bytes : 16, s));
   return DAWN_OK;
 }
 
