@@ -208,11 +208,14 @@ def alg_bytes(r, n, m):
     L2-sized at these graphs).
 
     bs_pull / bfs_pull (one bottom-up sweep): row_ptr 4(n+1) and the
-      columns of the unfinished rows 4*mu.
+      columns of the unfinished rows 4*mu.  bfs_step (single-source level
+      kernel) counts as bfs_pull at pull levels (mode 1), else as bfs_push.
     bs_push_scatter / bfs_push: row_ptr + col of the frontier rows 4*(nf + mf).
     bs_emit_dist: the 64 x n distance block written once.
     """
     k = r["kernel"]
+    if k == "bfs_step":  # the single-source level kernel: a pull or a push level by its mode
+        k = "bfs_pull" if r.get("mode") == 1 else "bfs_push"
     if k in ("bs_pull", "bfs_pull"):
         return 4 * (n + 1) + 4 * r["unvisited_edges"]
     if k in ("bs_push_scatter", "bfs_push"):

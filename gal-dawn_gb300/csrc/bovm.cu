@@ -80,16 +80,21 @@ __global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ ro
   ctl->n_pull = 0;
 }
 
-__global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ row_ptr,
-                                                   const int32_t* __restrict__ col, SsCtl* __restrict__ ctl,
-                                                   int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
-                                                   uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
-                                                   int32_t n, int32_t nwords) {
-  __shared__ int s_excl[kBlock / 32][32];
-  __shared__ int s_rs[kBlock / 32][32];
-  __shared__ int s_v[kBlock / 32][32];
-  __shared__ int32_t s_q[kBlock / 32][kWarpQueueBig];
-  if (ctl->done || ctl->mode != kModePush) return;
+// Shared memory of one level kernel: the push's row dealing and the
+// queue staging both directions use.
+struct LevelSmem {
+  int excl[kBlock / 32][32];
+  int rs[kBlock / 32][32];
+  int v[kBlock / 32][32];
+  int32_t q[kBlock / 32][kWarpQueueBig];
+};
+
+// Top-down level: the frontier's rows are dealt to warps; unvisited
+// targets are claimed in the visited bitmap and queued for the next level.
+__device__ __forceinline__ void push_level(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                                           SsCtl* __restrict__ ctl, int32_t* __restrict__ q,
+                                           Seg* __restrict__ segs, size_t segcap, uint32_t* __restrict__ vbm,
+                                           uint32_t* __restrict__ fbm, int32_t n, int32_t nwords, LevelSmem& sm) {
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
   const int32_t* qin = q + (size_t)pin * n;
@@ -108,7 +113,7 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
 
   unsigned long long my_mf = 0;
-  WarpQueueBig wq(s_q[wib], qout, qcount);
+  WarpQueueBig wq(sm.q[wib], qout, qcount);
   auto op = [&](int32_t, int k, bool valid) {
     const int32_t u = valid ? __ldg(col + k) : -1;
     const bool found = valid && claim_bit(vbm, u);
@@ -123,10 +128,20 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
     emit_routed(found, u, deg, rs, wq, sout, lpack);
   };
   seg_expand(row_ptr, sin, ln, op);
-  warp_expand(row_ptr, qin, qn, s_excl[wib], s_rs[wib], s_v[wib], op);
+  warp_expand(row_ptr, qin, qn, sm.excl[wib], sm.rs[wib], sm.v[wib], op);
   wq.flush();
   my_mf = warp_sum(my_mf);
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
+}
+
+__global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ row_ptr,
+                                                   const int32_t* __restrict__ col, SsCtl* __restrict__ ctl,
+                                                   int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
+                                                   uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
+                                                   int32_t n, int32_t nwords) {
+  __shared__ LevelSmem sm;
+  if (ctl->done || ctl->mode != kModePush) return;
+  push_level(row_ptr, col, ctl, q, segs, segcap, vbm, fbm, n, nwords, sm);
 }
 
 // Small frontiers: a single cluster of kSmallCtas CTAs runs push levels one
@@ -154,10 +169,13 @@ __global__ void __launch_bounds__(kBlock) bfs_push(const int32_t* __restrict__ r
 // The first level reads the global queue and segments the kernels before
 // wrote; its input counters are zeroed (behind one extra barrier) before a
 // later level of that parity can spill into them.
+__device__ __forceinline__ void decide_level(SsCtl* __restrict__ ctl, int32_t n, const float* __restrict__ sel_w,
+                                             cudaGraphConditionalHandle loop, int in_graph);
+
 __global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock)
     bfs_small(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col, SsCtl* ctl, int32_t* q,
               Seg* segs, size_t segcap, uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm, int32_t n,
-              int32_t nwords) {
+              int32_t nwords, const float* __restrict__ sel_w, cudaGraphConditionalHandle loop, int in_graph) {
   __shared__ SmallSlice s_sl[2];
   // per parity: vertices appended (past kSmallCap they spilled), whether
   // one has a row of >= kLongRow entries, and their out-degree sum (the
@@ -344,16 +362,24 @@ __global__ void __cluster_dims__(kSmallCtas, 1, 1) __launch_bounds__(kSmallBlock
     const int32_t v = __ldcg(&sl[i].v);
     if (i == 0 || __ldcg(&sl[i - 1].v) != v) atomicOr(fcur + (v >> 5), 1u << (v & 31));
   }
+  // The handed-off level's bookkeeping, as after a push level.  Every
+  // counter it reads was written before the cluster barrier above; it
+  // writes the other parity's counters and the level fields, which no CTA
+  // reads after that barrier.
+  if (rank == 0 && threadIdx.x < 32) {
+    __threadfence();
+    decide_level(ctl, n, sel_w, loop, in_graph);
+  }
 }
 
-__global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ row_ptr,
-                                                   const int32_t* __restrict__ t_row_ptr,
-                                                   const int32_t* __restrict__ t_col, SsCtl* __restrict__ ctl,
-                                                   int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
-                                                   uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
-                                                   int32_t n, int32_t nwords) {
-  __shared__ int32_t s_q[kBlock / 32][kWarpQueueBig];
-  if (ctl->done || ctl->mode != kModePull) return;
+// Bottom-up level: a warp owns 32 vertices (one bitmap word); each
+// unvisited one scans its in-edges until a frontier bit.
+__device__ __forceinline__ void pull_level(const int32_t* __restrict__ row_ptr,
+                                           const int32_t* __restrict__ t_row_ptr,
+                                           const int32_t* __restrict__ t_col, SsCtl* __restrict__ ctl,
+                                           int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
+                                           uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm, int32_t n,
+                                           int32_t nwords, LevelSmem& sm) {
   const int L = ctl->level;
   const int pout = L & 1;
   int32_t* qout = q + (size_t)pout * n;
@@ -370,7 +396,7 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nwords; i += gstride) fclr[i] = 0;
 
   unsigned long long my_mf = 0;
-  WarpQueueBig wq(s_q[threadIdx.x >> 5], qout, qcount);
+  WarpQueueBig wq(sm.q[threadIdx.x >> 5], qout, qcount);
   for (int w = global_warp(); w < nwords; w += num_warps()) {
     const uint32_t vis = vbm[w];
     uint32_t unv = ~vis;
@@ -408,23 +434,41 @@ __global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ r
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }
 
-// One warp.  Ends the loop when the frontier is empty, otherwise picks the
-// next level's direction: the forced variant if one is set, else the
-// learned selector if weights are loaded (direction-optimising calls only),
-// else Beamer's alpha/beta rule.
-__global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, const float* __restrict__ sel_w,
-                           cudaGraphConditionalHandle loop, int in_graph) {
-  const int lane = threadIdx.x;
+__global__ void __launch_bounds__(kBlock) bfs_pull(const int32_t* __restrict__ row_ptr,
+                                                   const int32_t* __restrict__ t_row_ptr,
+                                                   const int32_t* __restrict__ t_col, SsCtl* __restrict__ ctl,
+                                                   int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
+                                                   uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
+                                                   int32_t n, int32_t nwords) {
+  __shared__ LevelSmem sm;
+  if (ctl->done || ctl->mode != kModePull) return;
+  pull_level(row_ptr, t_row_ptr, t_col, ctl, q, segs, segcap, vbm, fbm, n, nwords, sm);
+}
+
+// One warp (all 32 lanes).  Ends the loop when the frontier is empty,
+// otherwise picks the next level's direction: the forced variant if one is
+// set, else the learned selector if weights are loaded (direction-
+// optimising calls only), else Beamer's alpha/beta rule.  The control block
+// is read through volatile loads: when this runs at the end of the level
+// kernel itself, counters other CTAs just raised may sit stale in this
+// SM's L1.
+__device__ __forceinline__ void decide_level(SsCtl* __restrict__ ctl, int32_t n, const float* __restrict__ sel_w,
+                                             cudaGraphConditionalHandle loop, int in_graph) {
+  const int lane = lane_id();
   if (sel_w) sel_prefetch(sel_w);
+  const volatile SsCtl* vc = ctl;
   // every lane reads the control block before lane 0 changes it
-  const int done = ctl->done;
-  const int L = ctl->level, pout = L & 1;
-  const int nf = ctl->qsize[pout] + long_vertices(ctl->lpack[pout]);
-  const unsigned long long mf = ctl->mf[pout];
-  const long long mu = ctl->mu - (long long)mf;
-  const int cur_mode = ctl->mode, prev_nf = ctl->prev_nf, policy = ctl->policy, force = ctl->force;
-  const bool sel = ctl->use_sel && sel_w;
-  const long long m = ctl->m;
+  const int done = vc->done;
+  const int L = vc->level, pout = L & 1;
+  const int nf = vc->qsize[pout] + long_vertices(vc->lpack[pout]);
+  const unsigned long long mf = vc->mf[pout];
+  const long long mu = vc->mu - (long long)mf;
+  const int cur_mode = vc->mode, prev_nf = vc->prev_nf, policy = vc->policy, force = vc->force;
+  const bool sel = vc->use_sel && sel_w;
+  const long long m = vc->m;
+  const int small = vc->small;
+  const unsigned long long nlong = long_vertices(vc->lpack[pout]);
+  const float margin = vc->sel_margin;
   __syncwarp();
   if (done) {
     if (lane == 0 && in_graph) cudaGraphSetConditional(loop, 0);
@@ -456,13 +500,13 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, const float* __re
     float x[kSelIn];
     sel_features(x, (float)n, (float)m, (float)nf, (float)mf, (float)mu, (float)(L + 1), (float)prev_nf, 1.0f);
     const int h = mode == kModePull ? kVarPull : kVarPush;
-    mode = sel_pick(sel_w, x, (1u << kVarPush) | (1u << kVarPull), h, ctl->sel_margin) == kVarPull ? kModePull
-                                                                                                : kModePush;
+    mode = sel_pick(sel_w, x, (1u << kVarPush) | (1u << kVarPull), h, margin) == kVarPull ? kModePull
+                                                                                         : kModePush;
   }
   // small levels start from frontiers without long rows: a long row's
   // neighbourhood tends to hold more, which end the cluster levels at once
-  if (mode == kModePush && ctl->small && !force && policy == DAWN_VARIANT_DO && nf <= kSmallFrontier &&
-      (long long)mf <= kSmallEdges && long_vertices(ctl->lpack[pout]) == 0)
+  if (mode == kModePush && small && !force && policy == DAWN_VARIANT_DO && nf <= kSmallFrontier &&
+      (long long)mf <= kSmallEdges && nlong == 0)
     mode = kModeSmall;
   if (lane == 0) {
     ctl->qsize[pout ^ 1] = 0;
@@ -471,6 +515,51 @@ __global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, const float* __re
     ctl->prev_nf = nf;
     ctl->mode = mode;
     ctl->level = L + 1;
+  }
+}
+
+__global__ void bfs_decide(SsCtl* __restrict__ ctl, int32_t n, const float* __restrict__ sel_w,
+                           cudaGraphConditionalHandle loop, int in_graph) {
+  decide_level(ctl, n, sel_w, loop, in_graph);
+}
+
+// One launch per push or pull level: the level's work, then its end-of-
+// level bookkeeping by the last CTA to finish (an arrival count in the
+// control block, reset by that CTA), so a level costs one kernel instead of
+// a work kernel and a decide kernel.  Returns at once at cluster levels.
+__global__ void __launch_bounds__(kBlock, 5) bfs_step(const int32_t* __restrict__ row_ptr,
+                                                   const int32_t* __restrict__ col,
+                                                   const int32_t* __restrict__ t_row_ptr,
+                                                   const int32_t* __restrict__ t_col, SsCtl* __restrict__ ctl,
+                                                   int32_t* __restrict__ q, Seg* __restrict__ segs, size_t segcap,
+                                                   uint32_t* __restrict__ vbm, uint32_t* __restrict__ fbm,
+                                                   int32_t n, int32_t nwords, const float* __restrict__ sel_w,
+                                                   cudaGraphConditionalHandle loop, int in_graph) {
+  __shared__ LevelSmem sm;
+  __shared__ int s_last;
+  if (ctl->done) {
+    // a traversal that ended before its first level (an isolated source)
+    // or at a cluster level: the loop still has to be told
+    if (in_graph && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(loop, 0);
+    return;
+  }
+  const int mode = ctl->mode;
+  if (mode == kModePush)
+    push_level(row_ptr, col, ctl, q, segs, segcap, vbm, fbm, n, nwords, sm);
+  else if (mode == kModePull)
+    pull_level(row_ptr, t_row_ptr, t_col, ctl, q, segs, segcap, vbm, fbm, n, nwords, sm);
+  else
+    return;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&ctl->arrive, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x < 32) {
+    __threadfence();
+    if (threadIdx.x == 0) ctl->arrive = 0;
+    decide_level(ctl, n, sel_w, loop, in_graph);
   }
 }
 
@@ -553,11 +642,10 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   a.in_graph = 0;
   void* clear_args[] = {&a.ctl, &a.bitmaps, &a.n, &a.nwords};
   void* init_args[] = {&a.ctl, &a.row_ptr, &a.q, &a.segs, &a.vbm, &a.n, &a.m};
-  void* push_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm, &a.n, &a.nwords};
-  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm,
-                       &a.n, &a.nwords};
-  void* small_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm, &a.n, &a.nwords};
-  void* decide_args[] = {&a.ctl, &a.n, &a.sel_w, &a.handle, &a.in_graph};
+  void* step_args[] = {&a.row_ptr, &a.col, &a.t_row_ptr, &a.t_col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm,
+                       &a.fbm, &a.n, &a.nwords, &a.sel_w, &a.handle, &a.in_graph};
+  void* small_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm, &a.n, &a.nwords,
+                        &a.sel_w, &a.handle, &a.in_graph};
   void* next_args[] = {&a.ctl};
 
   const int sms = g->geo.sms;
@@ -565,13 +653,15 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   fam.npre = 2;
   fam.pre[0] = {(const void*)bfs_clear, clear_args, dim3(sms * 4), dim3(kBlock)};
   fam.pre[1] = {(const void*)bfs_init, init_args, dim3(1), dim3(32)};
-  fam.nbody = 4;
-  fam.body[0] = {(const void*)bfs_push, push_args, dim3(persistent_blocks((const void*)bfs_push, kBlock, 0, g->blocks_per_sm)),
-                 dim3(kBlock), "bfs_push", kModePush};
-  fam.body[1] = {(const void*)bfs_pull, pull_args, dim3(persistent_blocks((const void*)bfs_pull, kBlock, 0, g->blocks_per_sm)),
-                 dim3(kBlock), "bfs_pull", kModePull};
-  fam.body[2] = {(const void*)bfs_small, small_args, dim3(kSmallCtas), dim3(kSmallBlock), "bfs_small", kModeSmall};
-  fam.body[3] = {(const void*)bfs_decide, decide_args, dim3(1), dim3(32), "bfs_decide"};
+  // Two kernels per loop iteration, each ending its level with the
+  // bookkeeping (no separate decide launch): the push/pull level kernel and
+  // the cluster levels; the one whose mode does not match returns at once.
+  fam.nbody = 2;
+  fam.decide_in_body = true;
+  fam.body[0] = {(const void*)bfs_step, step_args,
+                 dim3(persistent_blocks((const void*)bfs_step, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
+                 "bfs_step", kModeStep};
+  fam.body[1] = {(const void*)bfs_small, small_args, dim3(kSmallCtas), dim3(kSmallBlock), "bfs_small", kModeSmall};
   fam.npost = 1;
   fam.post[0] = {(const void*)ss_next, next_args, dim3(1), dim3(32), "ss_next"};
   fam.ctl = a.ctl;

@@ -64,6 +64,8 @@ void pool_free(void* p, cudaStream_t s);
 
 // kModeSmall: small frontiers, several push levels in one cluster launch
 enum : int32_t { kModePush = 0, kModePull = 1, kModeSmall = 2 };
+// Launch tag of a kernel that runs at push and at pull levels alike.
+constexpr int32_t kModeStep = 3;
 
 // Device-resident control block of one single-source traversal.  Every
 // per-level kernel reads its parameters from here, so the same launches
@@ -97,7 +99,8 @@ struct SsCtl {
   long long m;                  // CSR entries (selector input)
   // accumulated over all sources of the call
   unsigned long long total_reached;
-  int32_t total_levels, total_push, total_pull, pad2;
+  int32_t total_levels, total_push, total_pull;
+  int32_t arrive;               // CTAs of the running level kernel that finished (last one resets it)
 };
 
 // Kernel launches of one frontier-traversal family.  The driver runs them as
@@ -126,6 +129,9 @@ struct SsFamily {
   int npre = 0;
   Launch body[5];
   int nbody = 0;
+  // true: every body kernel ends its level with the bookkeeping itself;
+  // false: the last body kernel is the decide kernel, run at every level
+  bool decide_in_body = false;
   Launch post[2];
   int npost = 0;
   // the decide kernel (body[nbody-1]) takes these two arguments

@@ -308,14 +308,18 @@ dawn_status ss_run_traced(dawn_graph* g, SsFamily& fam, int32_t nruns) {
       if (p.done) break;
       Pending pend[5];
       int np = 0;
-      for (int b = 0; b + 1 < fam.nbody; b++) {
-        if (fam.body[b].mode >= 0 && fam.body[b].mode != p.mode) continue;
+      const int nwork = fam.decide_in_body ? fam.nbody : fam.nbody - 1;
+      for (int b = 0; b < nwork; b++) {
+        const int bm = fam.body[b].mode;
+        const bool match = bm < 0 || bm == p.mode || (bm == kModeStep && (p.mode == kModePush || p.mode == kModePull));
+        if (!match) continue;
         DAWN_CUDA(cudaEventRecord(g->trace_ev[2 * np], g->stream));
         DAWN_CHECK(launch(fam.body[b], g->stream, has_win ? &win : nullptr));
         DAWN_CUDA(cudaEventRecord(g->trace_ev[2 * np + 1], g->stream));
         pend[np++] = {b, p};
+        if (fam.decide_in_body) break;  // the kernel ran the level and its bookkeeping
       }
-      DAWN_CHECK(launch(fam.body[fam.nbody - 1], g->stream, has_win ? &win : nullptr));
+      if (!fam.decide_in_body) DAWN_CHECK(launch(fam.body[fam.nbody - 1], g->stream, has_win ? &win : nullptr));
       DAWN_CUDA(cudaStreamSynchronize(g->stream));
       for (int i = 0; i < np; i++) {
         dawn_trace_rec r = {};

@@ -20,6 +20,8 @@ def test_alg_bytes_per_kernel():
     assert bench.alg_bytes_with_words(pull, n, m) == 4 * (n + 1) + 16 * n + 4 * 5000
     single = dict(pull, kernel="bfs_pull")
     assert bench.alg_bytes(single, n, m) == 4 * (n + 1) + 4 * 5000
+    assert bench.alg_bytes(dict(pull, kernel="bfs_step", mode=1), n, m) == 4 * (n + 1) + 4 * 5000
+    assert bench.alg_bytes(dict(pull, kernel="bfs_step", mode=0), n, m) == 4 * (10 + 50)
     scatter = {"kernel": "bs_push_scatter", "frontier": 10, "frontier_edges": 50, "unvisited_edges": 0}
     assert bench.alg_bytes(scatter, n, m) == 4 * 60
     update = {"kernel": "bs_push_update", "frontier": 10, "frontier_edges": 5000, "unvisited_edges": 0}
