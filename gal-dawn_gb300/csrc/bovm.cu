@@ -43,10 +43,12 @@ __global__ void __launch_bounds__(kBlock) bfs_clear(SsCtl* __restrict__ ctl, uin
     bitmaps[i] = 0;
 }
 
-__global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
-                         int32_t* __restrict__ q, Seg* __restrict__ segs, uint32_t* __restrict__ vbm, int32_t n,
-                         long long m) {
-  if (threadIdx.x != 0) return;
+// The first level of the current source (one thread): distance 0, the
+// source in the visited bitmap and the level-0 frontier, its row as the
+// level-1 work, the level counters.
+__device__ __forceinline__ void init_source(SsCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
+                                            int32_t* __restrict__ q, Seg* __restrict__ segs,
+                                            uint32_t* __restrict__ vbm, int32_t n, long long m) {
   const int32_t s = ctl->sources[ctl->src_idx];
   int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
   const int32_t deg = row_ptr[s + 1] - row_ptr[s];
@@ -78,6 +80,45 @@ __global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ ro
   ctl->prev_nf = 1;
   ctl->n_push = 0;
   ctl->n_pull = 0;
+}
+
+__global__ void bfs_init(SsCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
+                         int32_t* __restrict__ q, Seg* __restrict__ segs, uint32_t* __restrict__ vbm, int32_t n,
+                         long long m) {
+  if (threadIdx.x != 0) return;
+  init_source(ctl, row_ptr, q, segs, vbm, n, m);
+}
+
+// bfs_clear and bfs_init in one launch: the distance row filled with -1
+// (16-byte stores over its aligned middle) and the bitmaps cleared, then
+// the last CTA to finish (arrival count in the control block, which it
+// resets) seeds the source.
+__global__ void __launch_bounds__(kBlock) bfs_start(SsCtl* __restrict__ ctl, const int32_t* __restrict__ row_ptr,
+                                                    int32_t* __restrict__ q, Seg* __restrict__ segs,
+                                                    uint32_t* __restrict__ bitmaps, int32_t n, int32_t nwords,
+                                                    long long m) {
+  __shared__ int s_last;
+  int32_t* dist = ctl->dist_base + (size_t)ctl->src_idx * n;
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+  const size_t head = ((16 - (reinterpret_cast<uintptr_t>(dist) & 15)) & 15) / 4;
+  const size_t h = head < (size_t)n ? head : (size_t)n;
+  const size_t nvec = ((size_t)n - h) / 4;
+  if (tid < h) dist[tid] = -1;
+  int4* d4 = reinterpret_cast<int4*>(dist + h);
+  for (size_t i = tid; i < nvec; i += stride) d4[i] = make_int4(-1, -1, -1, -1);
+  for (size_t i = h + 4 * nvec + tid; i < (size_t)n; i += stride) dist[i] = -1;
+  for (size_t i = tid; i < (size_t)4 * nwords; i += stride) bitmaps[i] = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&ctl->arrive, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last && threadIdx.x == 0) {
+    __threadfence();
+    ctl->arrive = 0;
+    init_source(ctl, row_ptr, q, segs, bitmaps, n, m);
+  }
 }
 
 // Shared memory of one level kernel: the push's row dealing and the
@@ -640,8 +681,7 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
   a.m = m;
   a.handle = 0;
   a.in_graph = 0;
-  void* clear_args[] = {&a.ctl, &a.bitmaps, &a.n, &a.nwords};
-  void* init_args[] = {&a.ctl, &a.row_ptr, &a.q, &a.segs, &a.vbm, &a.n, &a.m};
+  void* start_args[] = {&a.ctl, &a.row_ptr, &a.q, &a.segs, &a.bitmaps, &a.n, &a.nwords, &a.m};
   void* step_args[] = {&a.row_ptr, &a.col, &a.t_row_ptr, &a.t_col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm,
                        &a.fbm, &a.n, &a.nwords, &a.sel_w, &a.handle, &a.in_graph};
   void* small_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.q, &a.segs, &a.segcap, &a.vbm, &a.fbm, &a.n, &a.nwords,
@@ -650,9 +690,8 @@ dawn_status bfs_single(dawn_graph* g, const int32_t* sources, int32_t nsrc, int3
 
   const int sms = g->geo.sms;
   SsFamily fam;
-  fam.npre = 2;
-  fam.pre[0] = {(const void*)bfs_clear, clear_args, dim3(sms * 4), dim3(kBlock)};
-  fam.pre[1] = {(const void*)bfs_init, init_args, dim3(1), dim3(32)};
+  fam.npre = 1;
+  fam.pre[0] = {(const void*)bfs_start, start_args, dim3(sms * 8), dim3(kBlock), "bfs_start"};
   // Two kernels per loop iteration, each ending its level with the
   // bookkeeping (no separate decide launch): the push/pull level kernel and
   // the cluster levels; the one whose mode does not match returns at once.
