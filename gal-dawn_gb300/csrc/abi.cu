@@ -138,7 +138,7 @@ void destroy(dawn_graph* g) {
   dawn::pool_free(g->col, g->stream);
   if (g->val) dawn::pool_free(g->val, g->stream);
   DevBuf* bufs[] = {&g->ss_queues, &g->ss_segs, &g->bs_segs, &g->ss_bitmaps, &g->ss_ctl, &g->ss_sources, &g->ss_scratch,
-                    &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->cc_out,
+                    &g->bs_words, &g->bs_queues, &g->bs_ctl, &g->bs_sources, &g->ul_static, &g->hv_static, &g->hv_segoff, &g->hv_acc, &g->hv_tasks, &g->cc_out,
                     &g->dist_stage, &g->pt_voff, &g->pt_tasks, &g->pt_sources, &g->pt_ctl, &g->pt_scratch, &g->pt_rows,
                     &g->sel_slot, &g->wt_col, &g->wt_val, &g->mw_block, &g->mw_masks,
                     &g->mw_ctl, &g->mw_sources, &g->bc_levels, &g->bc_terms, &g->bc_range, &g->bc_out,

@@ -226,6 +226,7 @@ struct dawn_graph {
   dawn::DevBuf hv_static;       // heavy pull rows: in-degree >= kPullHeavy, id order
   dawn::DevBuf hv_segoff;       // exclusive prefix of their segment counts (nh + 1)
   dawn::DevBuf hv_acc;          // per heavy row: OR accumulator + finished-segment count
+  dawn::DevBuf hv_tasks;        // 2 x hv_segs (row, segment): segments of heavy rows still unfinished
   int32_t hv_count = 0, hv_segs = 0;
   int32_t bs_push_ratio = 4;    // push while ratio * frontier edges < unfinished edges
   int32_t bs_width = 0;         // words per vertex of the bitset traversal (0 = by source count)

@@ -52,6 +52,8 @@ struct BsCtl {
   int32_t push_ratio;           // push while push_ratio * frontier edges < unfinished edges
   int32_t work;                 // dynamic work counter of the current level (light rows)
   int32_t hwork;                // dynamic work counter of the heavy-row segments
+  int32_t hs_size[2];           // heavy-segment task lists: segments of rows still unfinished
+  int32_t hs_cur;               // list the next pull reads: -1 = every segment of the graph
   int32_t dense;                // push level: fire-and-forget scatter + dense update sweep
   int32_t nbits;                // level slices available
   int32_t width;                // W: words per vertex and state
@@ -370,6 +372,9 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     ctl->ul_size[0] = 0;
     ctl->ul_size[1] = 0;
     ctl->ul_cur = -1;
+    ctl->hs_size[0] = 0;
+    ctl->hs_size[1] = 0;
+    ctl->hs_cur = -1;
     ctl->work = 0;
     ctl->hwork = 0;
     ctl->dense = 0;
@@ -466,7 +471,8 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
                                                      const int32_t* __restrict__ ul_static, int32_t ul_static_size,
                                                      int32_t* __restrict__ ul, const int32_t* __restrict__ hv_static,
                                                      const int32_t* __restrict__ hv_segoff, u64* __restrict__ hv_acc,
-                                                     int32_t hv_count, int32_t hv_segs, int32_t pull_seg, int32_t n) {
+                                                     int2* __restrict__ hv_tasks, int32_t hv_count, int32_t hv_segs,
+                                                     int32_t pull_seg, int32_t n) {
   using B = Bits<W>;
   __shared__ int32_t s_qa[kBlock / 32][kWarpQueueBig];
   __shared__ int32_t s_qu[kBlock / 32][kWarpQueueBig];
@@ -494,16 +500,32 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
   WarpQueueBig qa(s_qa[wib], aq_out, aq_count);
   WarpQueueBig qu(s_qu[wib], ul_out, ul_count);
   const bool deep_cc = ctl->cc_sum && L >= kDeepLevel;
+  // Heavy-row segments: the first pull level deals every segment of the
+  // graph (finding its row by binary search); the finisher of a row that
+  // stays unfinished re-lists the row's segments as (row, segment) tasks,
+  // and later pull levels deal only those.
+  const int hcur = ctl->hs_cur;
+  const int hn = hcur < 0 ? hv_segs : ctl->hs_size[hcur];
+  const int2* __restrict__ hs_in = hv_tasks + (size_t)(hcur < 0 ? 0 : hcur) * hv_segs;
+  int2* hs_out = hv_tasks + (size_t)(hcur < 0 ? 0 : hcur ^ 1) * hv_segs;
+  int32_t* hs_count = &ctl->hs_size[hcur < 0 ? 0 : hcur ^ 1];
 
   for (;;) {
-    int sidx = 0;
-    if (lane == 0) sidx = atomicAdd(&ctl->hwork, 1);
-    sidx = __shfl_sync(kFull, sidx, 0);
-    if (sidx >= hv_segs) break;
-    int lo = 0, hi = hv_count - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(hv_segoff + mid) <= sidx) lo = mid; else hi = mid - 1;
+    int t = 0;
+    if (lane == 0) t = atomicAdd(&ctl->hwork, 1);
+    t = __shfl_sync(kFull, t, 0);
+    if (t >= hn) break;
+    int lo = 0, sidx = t;
+    if (hcur < 0) {
+      int hi = hv_count - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(hv_segoff + mid) <= sidx) lo = mid; else hi = mid - 1;
+      }
+    } else {
+      const int2 e = hs_in[t];
+      lo = e.x;
+      sidx = e.y;
     }
     const int32_t u = __ldg(hv_static + lo);
     const B vis = B::ld(visit + (size_t)u * W);
@@ -557,6 +579,14 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
         odeg = row_ptr[u + 1] - ors;
         acc.add((u64)odeg, (u64)(rend - rbeg), nw.popc(), (vis | nw) == full);
       }
+    }
+    // a row still missing bits keeps its segments for the next pull level
+    const B nw0 = nw.shfl(0);
+    if (!((vis | nw0) == full)) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(hs_count, nseg);
+      base = __shfl_sync(kFull, base, 0);
+      for (int j = lane; j < nseg; j += 32) hs_out[base + j] = make_int2(lo, s0 + j);
     }
     if (deep_cc) add_deep_sums<W>(ctl, nw, L);
     emit_routed(nw.any(), u, odeg, ors, qa, seg_out, al_pack);
@@ -1004,7 +1034,7 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, const float* __res
   // every lane reads the control block before lane 0 changes it
   const int done = ctl->done;
   const int L = ctl->level;
-  const int cur_mode = ctl->mode, ul_cur = ctl->ul_cur;
+  const int cur_mode = ctl->mode, ul_cur = ctl->ul_cur, hs_cur = ctl->hs_cur;
   const long long mu = ctl->mu - ctl->mu_dec;
   const int nf = ctl->aq_size[L % 3] + long_vertices(ctl->alpack[L % 3]);
   const long long mf = (long long)ctl->mf[L % 3];
@@ -1026,6 +1056,8 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, const float* __res
       ctl->n_pull++;
       ctl->ul_cur = ul_cur < 0 ? 0 : ul_cur ^ 1;
       ctl->ul_size[(ul_cur < 0 ? 0 : ul_cur ^ 1) ^ 1] = 0;
+      ctl->hs_cur = hs_cur < 0 ? 0 : hs_cur ^ 1;
+      ctl->hs_size[(hs_cur < 0 ? 0 : hs_cur ^ 1) ^ 1] = 0;
     }
     ctl->mu = mu;
     ctl->mu_dec = 0;
@@ -1122,6 +1154,10 @@ __global__ void scatter_flagged(const int64_t* __restrict__ flags, const int64_t
 // Static pull lists of the in-edge CSR (shared with the weighted pull).
 dawn_status build_static_list(dawn_graph* g) {
   if (g->ul_static.p && g->static_seg == g->pull_seg) return DAWN_OK;
+  // Captured traversal graphs (bitset and weighted single-source) hold these
+  // lists' addresses and sizes; a rebuild for a new segment size may move
+  // or resize them.
+  if (g->ul_static.p) drop_graphs(g);
   const int seg = g->pull_seg;
   const int32_t n = g->n;
   const size_t n1 = (size_t)n + 1;
@@ -1155,6 +1191,7 @@ dawn_status build_static_list(dawn_graph* g) {
                             g->stream));
   const size_t acc_bytes = sizeof(u64) * acc_stride(kMaxW) * (size_t)(cnt[1] > 0 ? cnt[1] : 1);
   DAWN_CHECK(ensure(g->hv_acc, acc_bytes, g->stream));
+  DAWN_CHECK(ensure(g->hv_tasks, sizeof(int2) * 2 * (size_t)(nseg > 0 ? nseg : 1), g->stream));
   DAWN_CUDA(cudaMemsetAsync(g->hv_acc.p, 0, acc_bytes, g->stream));
   pool_free(tmp, g->stream);
   DAWN_CUDA(cudaStreamSynchronize(g->stream));
@@ -1240,6 +1277,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
     int32_t ul_static_size, hv_count, hv_segs, pull_seg;
     const int32_t *hv_static, *hv_segoff;
     u64* hv_acc;
+    int2* hv_tasks;
     size_t nwords;
     int32_t n;
     long long m;
@@ -1258,6 +1296,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   a.hv_static = g->hv_static.as<int32_t>();
   a.hv_segoff = g->hv_segoff.as<int32_t>();
   a.hv_acc = g->hv_acc.as<u64>();
+  a.hv_tasks = g->hv_tasks.as<int2>();
   a.hv_count = g->hv_count;
   a.hv_segs = g->hv_segs;
   a.pull_seg = g->pull_seg;
@@ -1283,7 +1322,7 @@ dawn_status run_width(dawn_graph* g, const int32_t* sources, int32_t nsrc, int32
   void* init_args[] = {&a.ctl, &a.row_ptr, &a.t_row_ptr, &a.visit, &a.fr0, &a.aq0, &a.segs, &a.n, &a.m};
   void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.ctl, &a.visit, &a.fr, &a.slices, &a.aq, &a.segs,
                        &a.segcap, &a.ul_static, &a.ul_static_size, &a.ul, &a.hv_static, &a.hv_segoff,
-                       &a.hv_acc, &a.hv_count, &a.hv_segs, &a.pull_seg, &a.n};
+                       &a.hv_acc, &a.hv_tasks, &a.hv_count, &a.hv_segs, &a.pull_seg, &a.n};
   void* scatter_args[] = {&a.row_ptr, &a.col, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
                           &a.segcap, &a.tq, &a.tbm, &a.n};
   void* update_args[] = {&a.row_ptr, &a.t_row_ptr, &a.ctl, &a.visit, &a.fr, &a.nxt, &a.slices, &a.aq, &a.segs,
