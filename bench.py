@@ -53,15 +53,27 @@ METRIC = "GTEPS per GB300 (BFS/SSSP/MSSP) learned+batched vs plain; % HBM roofli
 L2_BYTES = 129 * 2 ** 20
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# headline step's kernels from one ncu capture, averaged over the launches of
-# one step.  Captured with:
-#   python bench.py --quick --traced --variant learned --steps 1 --warmup 1 &&
+# headline step's kernels from one ncu capture (GB300, 2026-12-04), averaged
+# over the launches of one step.  Captured with:
+#   python bench.py --quick --traced --variant bitset --steps 1 --warmup 1 &&
 #   ncu --nvtx --nvtx-include "dawn-step/" --clock-control none \
 #       --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum \
-#       --csv --log-file launches.csv python bench.py --quick --traced --variant learned --steps 1 --warmup 1
-# Keyed by kernel; a figure is reported only while the hash of the kernel's
-# source file matches the one it was captured on (None otherwise).
-NCU_TRAFFIC = {}
+#       --csv --log-file launches.csv python bench.py --quick --traced --variant bitset --steps 1 --warmup 1
+# Keyed by kernel; a figure is reported only while the SHA-256 prefix of the
+# kernel's source file matches the one it was captured on (None otherwise).
+_CAPTURE = ("ncu launch list of one RMAT-22 x 64 step, bitset variant, traced form: "
+            "dram__bytes_read.sum + dram__bytes_write.sum per launch")
+NCU_TRAFFIC = {
+    "bs_pull": {"bytes": 346.1e6, "launches": 5, "file": "gal-dawn_gb300/csrc/msbfs.cu", "sha": "e732f7ab85247f9f",
+                "source": _CAPTURE},
+    "bs_emit_dist": {"bytes": 1177.0e6, "launches": 1, "file": "gal-dawn_gb300/csrc/msbfs.cu",
+                     "sha": "e732f7ab85247f9f", "source": _CAPTURE},
+}
+# L1/TEX global-load sectors of the level-3 pull (every in-edge unfinished)
+# from `ncu --set full` of the same build (149,633,341 sectors, 128,306,834
+# in-edges): the unit the pull is bound by moves about one sector per SM
+# clock, so sectors per in-edge x in-edges / (SMs x clock) bounds a level.
+PULL_SECTORS_PER_EDGE = 149633341 / 128306834
 
 
 def _source_hash(path):
@@ -265,6 +277,18 @@ def kernel_roofline(recs, n, m, peak_gbs, peak_kind, skip=("bs_init", "bs_next")
     achieved = avg_bytes / (avg_ms * 1e-3) / 1e9
     achieved_w = k["bytes_w"] / k["launches"] / (avg_ms * 1e-3) / 1e9
     traffic = ncu_traffic(dom)
+    extra = {}
+    if dom == "bs_pull":
+        # the L1/TEX sector bound: one sector per SM per clock at the
+        # maximum SM clock, sectors per in-edge from the ncu capture
+        edges = sum(r["unvisited_edges"] for r in recs if r["kernel"] == dom)
+        launches = k["launches"]
+        sms, mhz = 152, 2070.0
+        floor_ms = PULL_SECTORS_PER_EDGE * edges / launches / (sms * mhz * 1e3)
+        extra["l1tex_bound"] = {"rule": "ncu sectors per in-edge x unfinished in-edges / (152 SMs x 1 sector per "
+                                        "clock x 2070 MHz), per launch",
+                                "floor_ms_per_launch": round(floor_ms, 4),
+                                "frac": round(floor_ms / avg_ms, 4)}
     return {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak_gbs,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": round(achieved / peak_gbs, 4),
             "traffic": int(traffic["bytes"]) if traffic else None,
@@ -275,7 +299,7 @@ def kernel_roofline(recs, n, m, peak_gbs, peak_kind, skip=("bs_init", "bs_next")
             "with_bitset_words": {"achieved": round(achieved_w, 1), "frac": round(achieved_w / peak_gbs, 4),
                                   "alg_bytes_per_launch": int(k["bytes_w"] / k["launches"])},
             "kernel_share": {name: round(v["ms"] / total, 4) for name, v in per.items()},
-            "source": "CUDA events around each kernel in a traced replay"}
+            "source": "CUDA events around each kernel in a traced replay", **extra}
 
 
 def traced(dg, run):
