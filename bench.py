@@ -1036,7 +1036,11 @@ def main():
     if checks:
         parity = {"config": f"rmat{args.scale} x {NSRC} sources", "equal": all(checks.values()),
                   "sources": NSRC, "against": cpu["kind"] + " MSSP_CPU::run", "checked": checks}
-    launches = len(recs) + 3  # level kernels + clear/init/next per batch (traced count)
+    # Kernels one graph-mode step launches: clear and init, the four body
+    # kernels (pull, push scatter, push update, decide) at every level (those
+    # of the other direction return at once), emit and next.
+    levels = len({(r["run"], r["level"]) for r in recs if r["level"] >= 1})
+    launches = 2 + 4 * levels + 2
     line = {"metric": METRIC, "value": round(value, 3), "unit": "GTEPS", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_step, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RMAT)",
