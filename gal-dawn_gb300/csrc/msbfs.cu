@@ -835,6 +835,58 @@ __device__ __forceinline__ void emit_vertex(int32_t* __restrict__ dist, int32_t 
   }
 }
 
+// emit_vertex4 without deep levels (no pair was written during the
+// traversal): the level of source s at vertex j is assembled from the level
+// slices eight sources at a time.  Byte c of slices 0-3 goes into one word
+// (slice k in byte k); for source 8c + i, ((word >> i) & 0x01010101) holds
+// the four level bits at bits 0, 8, 16, 24, and multiplying by 0x01020408
+// moves them to bits 24-27 without carries (every partial product lands on
+// a distinct bit, and only the four wanted ones land in bits 24-31).  A
+// fifth slice adds its bit separately; an unreached pair becomes -1 by
+// OR-ing (bit - 1).  About 8 instructions per (source, vertex) instead of
+// 19 with a shift and mask per slice.
+template <int W, int NB>
+__device__ __forceinline__ void emit_vertex4_packed(int32_t* __restrict__ dist, int32_t n, int nb_src, size_t u0,
+                                                    const u64* __restrict__ visit,
+                                                    const u64* __restrict__ slices) {
+#pragma unroll
+  for (int i = 0; i < W; i++) {
+    if (64 * i >= nb_src) break;
+    u64 vis[4], w[NB][4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      vis[j] = visit[(u0 + j) * W + i];
+#pragma unroll
+      for (int k = 0; k < NB; k++) w[k][j] = slices[((size_t)k * n + u0 + j) * W + i];
+    }
+    const int cnt = min(64, nb_src - 64 * i);
+    int32_t* row0 = dist + (size_t)(64 * i) * n + u0;
+    for (int c = 0; c < 8 && 8 * c < cnt; c++) {
+      uint32_t packed[4], five[4], vb[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        uint32_t x = 0;
+#pragma unroll
+        for (int k = 0; k < (NB < 4 ? NB : 4); k++) x |= (uint32_t)((w[k][j] >> (8 * c)) & 0xffull) << (8 * k);
+        packed[j] = x;
+        five[j] = NB > 4 ? (uint32_t)(w[NB > 4 ? 4 : 0][j] >> (8 * c)) & 0xffu : 0u;
+        vb[j] = (uint32_t)(vis[j] >> (8 * c)) & 0xffu;
+      }
+      const int lim = min(8, cnt - 8 * c);
+      for (int b = 0; b < lim; b++) {
+        int32_t v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          uint32_t x = (((packed[j] >> b) & 0x01010101u) * 0x01020408u) >> 24;
+          if (NB > 4) x |= ((five[j] >> b) & 1u) << 4;
+          v[j] = (int32_t)(x | (((vb[j] >> b) & 1u) - 1u));
+        }
+        *reinterpret_cast<int4*>(row0 + (size_t)(8 * c + b) * n) = make_int4(v[0], v[1], v[2], v[3]);
+      }
+    }
+  }
+}
+
 // Four consecutive vertices u0..u0+3 per thread: every source row gets one
 // 16-byte store, so a warp writes 512 contiguous bytes per row (needs n and
 // the output base 16-byte aligned, which the caller checks).  Rows holding a
@@ -999,6 +1051,18 @@ __global__ void __launch_bounds__(kBlock) bs_emit_dist(const BsCtl* __restrict__
   }
   int32_t* dist = ctl->dist_base + (size_t)batch * per * n;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
+  if ((n & 3) == 0 && (reinterpret_cast<uintptr_t>(dist) & 15) == 0 && !src) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)n / 4; q += stride) {
+      switch (nbits) {
+        case 1: emit_vertex4_packed<W, 1>(dist, n, nb, 4 * q, visit, slices); break;
+        case 2: emit_vertex4_packed<W, 2>(dist, n, nb, 4 * q, visit, slices); break;
+        case 3: emit_vertex4_packed<W, 3>(dist, n, nb, 4 * q, visit, slices); break;
+        case 4: emit_vertex4_packed<W, 4>(dist, n, nb, 4 * q, visit, slices); break;
+        default: emit_vertex4_packed<W, 5>(dist, n, nb, 4 * q, visit, slices); break;
+      }
+    }
+    return;
+  }
   if ((n & 3) == 0 && (reinterpret_cast<uintptr_t>(dist) & 15) == 0) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)n / 4; q += stride) {
       switch (nbits) {
