@@ -64,10 +64,10 @@ L2_BYTES = 129 * 2 ** 20
 _CAPTURE = ("ncu launch list of one RMAT-22 x 64 step, bitset variant, traced form: "
             "dram__bytes_read.sum + dram__bytes_write.sum per launch")
 NCU_TRAFFIC = {
-    "bs_pull": {"bytes": 346.1e6, "launches": 5, "file": "gal-dawn_gb300/csrc/msbfs.cu", "sha": "e732f7ab85247f9f",
+    "bs_pull": {"bytes": 342.1e6, "launches": 5, "file": "gal-dawn_gb300/csrc/msbfs.cu", "sha": "c1debad809378c50",
                 "source": _CAPTURE},
-    "bs_emit_dist": {"bytes": 1177.0e6, "launches": 1, "file": "gal-dawn_gb300/csrc/msbfs.cu",
-                     "sha": "e732f7ab85247f9f", "source": _CAPTURE},
+    "bs_emit_dist": {"bytes": 1177.6e6, "launches": 1, "file": "gal-dawn_gb300/csrc/msbfs.cu",
+                     "sha": "c1debad809378c50", "source": _CAPTURE},
 }
 # L1/TEX global-load sectors of the level-3 pull (every in-edge unfinished)
 # from `ncu --set full` of the same build (149,633,341 sectors, 128,306,834
