@@ -76,6 +76,11 @@ struct BsCtl {
   long long m;                  // CSR entries (selector input)
   unsigned long long total_reached;
   int32_t total_levels, total_push, total_pull, pad2;
+  // 1 = the level that wrote this slot's frontier words kept no active list
+  // (a dense push update: the next level is then a pull, which needs none,
+  // and the slot is cleared densely when it goes stale); aq_size holds the
+  // count only
+  int32_t unlisted[3], pad5;
 };
 
 constexpr int kSlicesCleared = 4;  // slices zeroed per batch; higher ones on first use
@@ -319,8 +324,8 @@ __device__ __forceinline__ void ld_col8(const int32_t* p, uint64_t pol, int32_t 
 // that many scattered partial-sector writes.
 template <int W>
 __device__ __forceinline__ void clear_stale(u64* __restrict__ fr, int32_t n, const int32_t* __restrict__ list,
-                                            int cnt, const Seg* __restrict__ segs, int nsegs) {
-  if ((long long)cnt * 4 <= n) {
+                                            int cnt, const Seg* __restrict__ segs, int nsegs, bool unlisted) {
+  if (!unlisted && (long long)cnt * 4 <= n) {
     clear_listed<W>(fr, list, cnt, segs, nsegs);
     return;
   }
@@ -372,6 +377,7 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     ctl->ul_size[0] = 0;
     ctl->ul_size[1] = 0;
     ctl->ul_cur = -1;
+    ctl->unlisted[0] = ctl->unlisted[1] = ctl->unlisted[2] = 0;
     ctl->hs_size[0] = 0;
     ctl->hs_size[1] = 0;
     ctl->hs_cur = -1;
@@ -485,7 +491,8 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
   int32_t* aq_count = &ctl->aq_size[L % 3];
   u64* al_pack = &ctl->alpack[L % 3];
   clear_stale<W>(fr + (size_t)((L + 1) % 3) * n * W, n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
-                 segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
+                 segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]),
+                 ctl->unlisted[(L + 1) % 3] != 0);
   const uint64_t pol = evict_first_policy();
   clear_next_slice<W>(slices, n, L, ctl->nbits);
   const int cur = ctl->ul_cur;
@@ -703,7 +710,8 @@ __global__ void __launch_bounds__(kBlock) bs_push_scatter(const int32_t* __restr
   const int ln = seg_count(ctl->alpack[(L - 1) % 3]);
   const bool dense = ctl->dense != 0;
   clear_stale<W>(fr + (size_t)((L + 1) % 3) * n * W, n, aq + (size_t)((L + 1) % 3) * n, ctl->aq_size[(L + 1) % 3],
-                 segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]));
+                 segs + (size_t)((L + 1) % 3) * segcap, seg_count(ctl->alpack[(L + 1) % 3]),
+                 ctl->unlisted[(L + 1) % 3] != 0);
   clear_next_slice<W>(slices, n, L, ctl->nbits);
   const int wib = threadIdx.x >> 5;
   // The first two levels expand the sources and their neighbours, whose
@@ -766,6 +774,13 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
   const B full = B::full_of(ctl);
   const bool dense = ctl->dense != 0;
   const int tn = dense ? n : ctl->tq_size;
+  // A dense level's output frontier is large enough that the next level is
+  // a pull (the decide kernel makes it one), which reads frontier words,
+  // not an active list: the sweep then only counts the frontier instead of
+  // queueing it and cutting its long rows into segments.  Forced-variant
+  // runs keep the list (a forced push reads it).
+  const bool lazy = dense && !ctl->force;
+  int my_nf = 0;
   WarpQueueBig wq(s_q[threadIdx.x >> 5], aq_out, &ctl->aq_size[L % 3]);
   LevelAcc acc;
   const bool deep_cc = ctl->cc_sum && L >= kDeepLevel;
@@ -794,10 +809,17 @@ __global__ void __launch_bounds__(kBlock) bs_push_update(const int32_t* __restri
       }
     }
     if (deep_cc) add_deep_sums<W>(ctl, nw, L);
-    emit_routed(nw.any(), u, odeg, ors, wq, seg_out, &ctl->alpack[L % 3]);
+    if (lazy)
+      my_nf += __popc(__ballot_sync(kFull, nw.any()));
+    else
+      emit_routed(nw.any(), u, odeg, ors, wq, seg_out, &ctl->alpack[L % 3]);
   }
   wq.flush();
   acc.flush(ctl, L % 3);
+  if (lazy) {
+    if (lane_id() == 0 && my_nf) atomicAdd(&ctl->aq_size[L % 3], my_nf);
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->unlisted[L % 3] = 1;
+  }
 }
 
 // Expands the level slices of one batch into its distance rows: thread per
@@ -1101,6 +1123,7 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, const float* __res
   const int cur_mode = ctl->mode, ul_cur = ctl->ul_cur, hs_cur = ctl->hs_cur;
   const long long mu = ctl->mu - ctl->mu_dec;
   const int nf = ctl->aq_size[L % 3] + long_vertices(ctl->alpack[L % 3]);
+  const bool unlisted = ctl->unlisted[L % 3] != 0;
   const long long mf = (long long)ctl->mf[L % 3];
   const int policy = ctl->policy, ratio = ctl->push_ratio, force = ctl->force, prev_nf = ctl->prev_nf;
   const bool sel = ctl->use_sel && sel_w;
@@ -1155,11 +1178,13 @@ __global__ void bs_decide(BsCtl* __restrict__ ctl, int32_t n, const float* __res
     const unsigned allowed = policy == DAWN_VARIANT_PUSH ? (1u << kVarPush) | (1u << kVarDense) : 7u;
     variant = sel_pick(sel_w, x, allowed, variant, sel_margin);
   }
+  if (unlisted) variant = kVarPull;  // no active list to push from (never with a forced variant)
   if (lane == 0) {
     // Level L+1 writes list (L+1)%3, whose stale frontier words level L cleared.
     ctl->aq_size[(L + 1) % 3] = 0;
     ctl->alpack[(L + 1) % 3] = 0;
     ctl->mf[(L + 1) % 3] = 0;
+    ctl->unlisted[(L + 1) % 3] = 0;
     ctl->dense = variant == kVarDense;
     ctl->mode = variant == kVarPull ? kModePull : kModePush;
     ctl->prev_nf = nf;
