@@ -507,6 +507,13 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
   WarpQueueBig qa(s_qa[wib], aq_out, aq_count);
   WarpQueueBig qu(s_qu[wib], ul_out, ul_count);
   const bool deep_cc = ctl->cc_sum && L >= kDeepLevel;
+  // A pull level entered with a frontier of at least n / 16 vertices keeps
+  // no active list: its output frontier is counted, the next level is made
+  // a pull (which reads frontier words), and the slot is cleared densely
+  // when it goes stale.  Smaller levels queue their output for a push.
+  const long long nf_in = (long long)ctl->aq_size[(L - 1) % 3] + long_vertices(ctl->alpack[(L - 1) % 3]);
+  const bool lazy = !ctl->force && nf_in * 16 >= n;
+  int my_nf = 0;
   // Heavy-row segments: the first pull level deals every segment of the
   // graph (finding its row by binary search); the finisher of a row that
   // stays unfinished re-lists the row's segments as (row, segment) tasks,
@@ -596,7 +603,10 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
       for (int j = lane; j < nseg; j += 32) hs_out[base + j] = make_int2(lo, s0 + j);
     }
     if (deep_cc) add_deep_sums<W>(ctl, nw, L);
-    emit_routed(nw.any(), u, odeg, ors, qa, seg_out, al_pack);
+    if (lazy)
+      my_nf += __popc(__ballot_sync(kFull, nw.any()));
+    else
+      emit_routed(nw.any(), u, odeg, ors, qa, seg_out, al_pack);
   }
 
   for (;;) {
@@ -675,11 +685,18 @@ __global__ void __launch_bounds__(kBlock, W == 1 ? 5 : 4) bs_pull(const int32_t*
     }
     if (deep_cc) add_deep_sums<W>(ctl, nw, L);
     qu.push(still, u);
-    emit_routed(has, u, odeg, ors, qa, seg_out, al_pack);
+    if (lazy)
+      my_nf += __popc(__ballot_sync(kFull, has));
+    else
+      emit_routed(has, u, odeg, ors, qa, seg_out, al_pack);
   }
   qa.flush();
   qu.flush();
   acc.flush(ctl, L % 3);
+  if (lazy) {
+    if (lane == 0 && my_nf) atomicAdd(aq_count, my_nf);
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->unlisted[L % 3] = 1;
+  }
 }
 
 // Push, phase 1: the active vertices' rows (short rows warp-cooperatively,
