@@ -45,11 +45,14 @@ struct MwCtl {
   unsigned long long lpack[2];
   unsigned long long mf[2];
   int32_t level, done, batch, nsrc;
+  int32_t mode;                 // kModePush or kModePull for the next level
+  int32_t work, hwork;          // pull: dynamic work counters (light rows, heavy-row segments)
+  int32_t n_pull;
   int32_t n_push, inits;       // inits: mw_init CTAs finished
   unsigned long long reached;   // TEPS numerator of all batches so far
   int32_t* dist_base;           // nsrc x n output (source-major)
   const int32_t* sources;
-  int32_t total_levels, total_push;
+  int32_t total_levels, total_push, total_pull;
 };
 
 __device__ __forceinline__ int32_t relax(int32_t d, int32_t w, bool is_float) {
@@ -69,7 +72,11 @@ __global__ void __launch_bounds__(kBlock) mw_clear(MwCtl* __restrict__ ctl, int3
     ctl->level = 1;
     ctl->done = 0;
     ctl->n_push = 0;
+    ctl->n_pull = 0;
     ctl->inits = 0;
+    ctl->mode = kModePush;
+    ctl->work = 0;
+    ctl->hwork = 0;
   }
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   int4* d4 = reinterpret_cast<int4*>(D);
@@ -232,7 +239,7 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
                                                   unsigned long long* __restrict__ masks, int32_t* __restrict__ q,
                                                   Seg* __restrict__ segs, size_t segcap, int32_t n) {
   __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
-  if (ctl->done) return;
+  if (ctl->done || ctl->mode != kModePush) return;
   const int L = ctl->level;
   const int pin = (L - 1) & 1, pout = L & 1;
   const unsigned long long* __restrict__ m_in = masks + (size_t)((L - 1) % 3) * n;
@@ -343,19 +350,174 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
   if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
 }
 
-__global__ void mw_decide(MwCtl* __restrict__ ctl, int32_t n, cudaGraphConditionalHandle loop, int in_graph) {
+// Pull level (frontiers whose out-edges reach half the graph): every vertex
+// v takes, per source, the minimum of D[u][s] + w over its in-edges (u, w)
+// from tails whose source s improved at the last level, and keeps it where
+// it beats D[v][s].  A warp owns a light row (in-degree below 2 x pull_seg)
+// and writes its row of D and its next mask with plain stores: no atomics
+// per edge, and one improvement ballot per vertex instead of per edge.
+// Heavy rows are cut into pull_seg-entry segment tasks, each a warp, which
+// lower the row with return-free atomicMin where they improve on it and
+// OR their improved sources into the next mask (the first setter queues
+// the vertex).  Lane i owns sources i and i + 32, as in the push.  Tails
+// are read 32 at a time (vertex, weight and mask coalesced or gathered once
+// per lane), then four distance rows are fetched before any is used.
+// Reading a row that another warp lowers in the same level is harmless:
+// every value a row holds is the length of some path, and a value lowered
+// now is relaxed again at the next level through the mask it sets.
+__device__ __forceinline__ void pull_min(const int32_t* __restrict__ t_col, const int32_t* __restrict__ t_w,
+                                         const unsigned long long* __restrict__ m_in,
+                                         const int32_t* __restrict__ D, bool fl, int k0, int k1,
+                                         int32_t& minA, int32_t& minB) {
+  const int lane = lane_id();
+  for (int kb = k0; kb < k1; kb += 32) {
+    const int k = kb + lane;
+    const int32_t cu = k < k1 ? __ldg(t_col + k) : -1;
+    const int32_t cw = k < k1 ? __ldg(t_w + k) : 0;
+    const unsigned long long cm = cu >= 0 ? __ldcg(m_in + cu) : 0ull;
+    unsigned live = __ballot_sync(kFull, cm != 0ull);
+    while (live) {
+      int32_t u[kUnroll], w[kUnroll], dA[kUnroll], dB[kUnroll];
+      unsigned long long mk[kUnroll];
+#pragma unroll
+      for (int i = 0; i < kUnroll; i++) {
+        const int j = live ? __ffs(live) - 1 : 0;
+        const bool ok = live != 0;
+        live &= live - 1;
+        u[i] = __shfl_sync(kFull, cu, j);
+        w[i] = __shfl_sync(kFull, cw, j);
+        mk[i] = __shfl_sync(kFull, cm, j);
+        if (!ok) mk[i] = 0ull;
+      }
+#pragma unroll
+      for (int i = 0; i < kUnroll; i++) {
+        const int32_t* du = D + (size_t)(u[i] < 0 ? 0 : u[i]) * kBatch;
+        dA[i] = (mk[i] >> lane) & 1ull ? __ldcg(du + lane) : 0x7fffffff;
+        dB[i] = (mk[i] >> (lane + 32)) & 1ull ? __ldcg(du + lane + 32) : 0x7fffffff;
+      }
+#pragma unroll
+      for (int i = 0; i < kUnroll; i++) {
+        if ((mk[i] >> lane) & 1ull) minA = min(minA, relax(dA[i], w[i], fl));
+        if ((mk[i] >> (lane + 32)) & 1ull) minB = min(minB, relax(dB[i], w[i], fl));
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__ row_ptr,
+                                                  const int32_t* __restrict__ t_row_ptr,
+                                                  const int32_t* __restrict__ t_col, const int32_t* __restrict__ t_w,
+                                                  int is_float, MwCtl* __restrict__ ctl, int32_t* __restrict__ D,
+                                                  unsigned long long* __restrict__ masks, int32_t* __restrict__ q,
+                                                  Seg* __restrict__ segs, size_t segcap,
+                                                  const int32_t* __restrict__ ul, int32_t ul_n,
+                                                  const int32_t* __restrict__ hv, const int32_t* __restrict__ hv_segoff,
+                                                  int32_t hv_count, int32_t hv_segs, int32_t pull_seg, int32_t n) {
+  __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  if (ctl->done || ctl->mode != kModePull) return;
+  const int L = ctl->level;
+  const int pout = L & 1;
+  const unsigned long long* __restrict__ m_in = masks + (size_t)((L - 1) % 3) * n;
+  unsigned long long* m_out = masks + (size_t)(L % 3) * n;
+  {
+    unsigned long long* m_clr = masks + (size_t)((L + 1) % 3) * n;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)n; i += stride) m_clr[i] = 0ull;
+  }
+  const int lane = lane_id(), wib = threadIdx.x >> 5;
+  const bool fl = is_float != 0;
+  WarpQueue wq(s_q[wib], q + (size_t)pout * n, &ctl->qsize[pout]);
+  Seg* sout = segs + (size_t)pout * segcap;
+  unsigned long long* lpack = &ctl->lpack[pout];
+  unsigned long long my_mf = 0;
+
+  // heavy rows: segment tasks
+  for (;;) {
+    int sidx = 0;
+    if (lane == 0) sidx = atomicAdd(&ctl->hwork, 1);
+    sidx = __shfl_sync(kFull, sidx, 0);
+    if (sidx >= hv_segs) break;
+    int lo = 0, hi = hv_count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(hv_segoff + mid) <= sidx) lo = mid; else hi = mid - 1;
+    }
+    const int32_t v = __ldg(hv + lo);
+    const int rbeg = t_row_ptr[v], rend = t_row_ptr[v + 1];
+    const int ks = rbeg + (sidx - __ldg(hv_segoff + lo)) * pull_seg, ke = min(ks + pull_seg, rend);
+    int32_t minA = 0x7fffffff, minB = 0x7fffffff;
+    pull_min(t_col, t_w, m_in, D, fl, ks, ke, minA, minB);
+    int32_t* dv = D + (size_t)v * kBatch;
+    const bool impA = minA < __ldcg(dv + lane), impB = minB < __ldcg(dv + lane + 32);
+    if (impA) atomicMin(dv + lane, minA);
+    if (impB) atomicMin(dv + lane + 32, minB);
+    const unsigned long long bits = (unsigned long long)__ballot_sync(kFull, impA) |
+                                    ((unsigned long long)__ballot_sync(kFull, impB) << 32);
+    bool first = false;
+    int deg = 0, rs = 0;
+    if (bits && lane == 0) {
+      first = atomicOr(m_out + v, bits) == 0ull;
+      if (first) {
+        rs = row_ptr[v];
+        deg = row_ptr[v + 1] - rs;
+        my_mf += (unsigned long long)deg;
+      }
+    }
+    emit_routed(first, v, deg, rs, wq, sout, lpack);
+  }
+
+  // light rows: 32 list entries per warp task, one vertex after another
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&ctl->work, 32);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= ul_n) break;
+    const int cnt = min(32, ul_n - base);
+    const int32_t mine = lane < cnt ? __ldg(ul + base + lane) : -1;
+    for (int j = 0; j < cnt; j++) {
+      const int32_t v = __shfl_sync(kFull, mine, j);
+      const int k0 = t_row_ptr[v], k1 = t_row_ptr[v + 1];
+      int32_t minA = 0x7fffffff, minB = 0x7fffffff;
+      pull_min(t_col, t_w, m_in, D, fl, k0, k1, minA, minB);
+      int32_t* dv = D + (size_t)v * kBatch;
+      const bool impA = minA < __ldcg(dv + lane), impB = minB < __ldcg(dv + lane + 32);
+      if (impA) dv[lane] = minA;
+      if (impB) dv[lane + 32] = minB;
+      const unsigned long long bits = (unsigned long long)__ballot_sync(kFull, impA) |
+                                      ((unsigned long long)__ballot_sync(kFull, impB) << 32);
+      int deg = 0, rs = 0;
+      if (bits) {
+        if (lane == 0) m_out[v] = bits;
+        rs = row_ptr[v];
+        deg = row_ptr[v + 1] - rs;
+        if (lane == 0) my_mf += (unsigned long long)deg;
+      }
+      emit_routed(bits != 0ull && lane == 0, v, deg, rs, wq, sout, lpack);
+    }
+  }
+  wq.flush();
+  my_mf = warp_sum(my_mf);
+  if (lane == 0 && my_mf) atomicAdd(&ctl->mf[pout], my_mf);
+}
+
+__global__ void mw_decide(MwCtl* __restrict__ ctl, int32_t n, long long m, int can_pull,
+                          cudaGraphConditionalHandle loop, int in_graph) {
   if (threadIdx.x != 0) return;
   if (ctl->done) {
     if (in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
   const int L = ctl->level, pout = L & 1;
-  ctl->n_push++;
+  if (ctl->mode == kModePull) ctl->n_pull++; else ctl->n_push++;
   if ((ctl->qsize[pout] == 0 && ctl->lpack[pout] == 0) || L >= n) {
     ctl->done = 1;
     if (in_graph) cudaGraphSetConditional(loop, 0);
     return;
   }
+  // a frontier whose out-edges reach half the graph is relaxed by a pull
+  ctl->mode = can_pull && 2 * (long long)ctl->mf[pout] >= m ? kModePull : kModePush;
+  ctl->work = 0;
+  ctl->hwork = 0;
   ctl->qsize[pout ^ 1] = 0;
   ctl->lpack[pout ^ 1] = 0;
   ctl->mf[pout ^ 1] = 0;
@@ -422,6 +584,7 @@ __global__ void mw_next(MwCtl* __restrict__ ctl) {
   if (threadIdx.x != 0) return;
   ctl->total_levels += ctl->level;
   ctl->total_push += ctl->n_push;
+  ctl->total_pull += ctl->n_pull;
   ctl->batch += 1;
 }
 
@@ -429,7 +592,7 @@ void probe_mw(const void* p, LevelProbe* out) {
   const MwCtl* c = static_cast<const MwCtl*>(p);
   const int pin = (c->level - 1) & 1;
   out->level = c->level;
-  out->mode = kModePush;
+  out->mode = c->mode;
   out->done = c->done;
   out->frontier = c->qsize[pin] + (int64_t)(c->lpack[pin] >> 32);
   out->frontier_edges = (int64_t)c->mf[pin];
@@ -449,6 +612,9 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
   DAWN_CHECK(ensure(g->ss_segs, sizeof(Seg) * 2 * segcap, g->stream));
   DAWN_CHECK(ensure(g->mw_ctl, sizeof(MwCtl), g->stream));
   DAWN_CHECK(ensure(g->mw_sources, sizeof(int32_t) * (size_t)nsrc, g->stream));
+  // pull levels read in-edges with their weights and the in-degree lists
+  DAWN_CHECK(build_weighted_in_edges(g));
+  DAWN_CHECK(build_static_list(g));
   DAWN_CUDA(cudaMemcpyAsync(g->mw_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
                             g->stream));
   MwCtl c = {};
@@ -469,7 +635,22 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
     int32_t n, inf;
     cudaGraphConditionalHandle handle;
     int in_graph;
+    const int32_t *t_row_ptr, *t_col, *t_w, *ul, *hv, *hv_segoff;
+    int32_t ul_n, hv_count, hv_segs, pull_seg, can_pull;
+    long long m;
   } a;
+  a.t_row_ptr = g->t_row_ptr;
+  a.t_col = g->wt_col.as<int32_t>();
+  a.t_w = g->wt_val.as<int32_t>();  // int32 weights or float32 bit patterns, in in-edge order
+  a.ul = g->ul_static.as<int32_t>();
+  a.hv = g->hv_static.as<int32_t>();
+  a.hv_segoff = g->hv_segoff.as<int32_t>();
+  a.ul_n = g->ul_static_size;
+  a.hv_count = g->hv_count;
+  a.hv_segs = g->hv_segs;
+  a.pull_seg = g->pull_seg;
+  a.can_pull = 1;
+  a.m = g->m;
   a.ctl = g->mw_ctl.as<MwCtl>();
   a.row_ptr = g->row_ptr;
   a.col = g->col;
@@ -490,7 +671,10 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
   void* init_args[] = {&a.ctl, &a.row_ptr, &a.col, &a.w, &a.D, &a.masks, &a.q, &a.segs};
   void* push_args[] = {&a.row_ptr, &a.col, &a.w, &a.is_float, &a.ctl, &a.D, &a.masks, &a.q, &a.segs, &a.segcap,
                        &a.n};
-  void* decide_args[] = {&a.ctl, &a.n, &a.handle, &a.in_graph};
+  void* pull_args[] = {&a.row_ptr, &a.t_row_ptr, &a.t_col, &a.t_w, &a.is_float, &a.ctl, &a.D, &a.masks, &a.q,
+                       &a.segs, &a.segcap, &a.ul, &a.ul_n, &a.hv, &a.hv_segoff, &a.hv_count, &a.hv_segs,
+                       &a.pull_seg, &a.n};
+  void* decide_args[] = {&a.ctl, &a.n, &a.m, &a.can_pull, &a.handle, &a.in_graph};
   void* emit_args[] = {&a.ctl, &a.D, &a.row_ptr, &a.inf, &a.n};
   void* next_args[] = {&a.ctl};
   const int sms = g->geo.sms;
@@ -498,11 +682,14 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
   fam.npre = 2;
   fam.pre[0] = {(const void*)mw_clear, clear_args, dim3(sms * 8), dim3(kBlock), "mw_clear"};
   fam.pre[1] = {(const void*)mw_init, init_args, dim3(kBatch), dim3(kInitBlock), "mw_init"};
-  fam.nbody = 2;
+  fam.nbody = 3;
   fam.body[0] = {(const void*)mw_push, push_args,
                  dim3(persistent_blocks((const void*)mw_push, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
                  "mw_push", kModePush};
-  fam.body[1] = {(const void*)mw_decide, decide_args, dim3(1), dim3(32), "mw_decide"};
+  fam.body[1] = {(const void*)mw_pull, pull_args,
+                 dim3(persistent_blocks((const void*)mw_pull, kBlock, 0, g->blocks_per_sm)), dim3(kBlock),
+                 "mw_pull", kModePull};
+  fam.body[2] = {(const void*)mw_decide, decide_args, dim3(1), dim3(32), "mw_decide"};
   fam.npost = 2;
   fam.post[0] = {(const void*)mw_emit, emit_args, dim3(sms * 8), dim3(kEmitBlock), "mw_emit"};
   fam.post[1] = {(const void*)mw_next, next_args, dim3(1), dim3(32), "mw_next"};
@@ -527,7 +714,7 @@ dawn_status sssp_batched_stats(dawn_graph* g, dawn_stats* st, int32_t nsrc) {
   st->edges_traversed = (int64_t)h.reached;
   st->levels = h.total_levels;
   st->push_levels = h.total_push;
-  st->pull_levels = 0;
+  st->pull_levels = h.total_pull;
   st->batches = (nsrc + kBatch - 1) / kBatch;
   return DAWN_OK;
 }
