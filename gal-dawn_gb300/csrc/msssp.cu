@@ -365,6 +365,8 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
 // Reading a row that another warp lowers in the same level is harmless:
 // every value a row holds is the length of some path, and a value lowered
 // now is relaxed again at the next level through the mask it sets.
+constexpr int kPullUnroll = 4;  // distance rows of the pull fetched together
+
 __device__ __forceinline__ void pull_min(const int32_t* __restrict__ t_col, const int32_t* __restrict__ t_w,
                                          const unsigned long long* __restrict__ m_in,
                                          const int32_t* __restrict__ D, bool fl, int k0, int k1,
@@ -377,10 +379,10 @@ __device__ __forceinline__ void pull_min(const int32_t* __restrict__ t_col, cons
     const unsigned long long cm = cu >= 0 ? __ldcg(m_in + cu) : 0ull;
     unsigned live = __ballot_sync(kFull, cm != 0ull);
     while (live) {
-      int32_t u[kUnroll], w[kUnroll], dA[kUnroll], dB[kUnroll];
-      unsigned long long mk[kUnroll];
+      int32_t u[kPullUnroll], w[kPullUnroll], dA[kPullUnroll], dB[kPullUnroll];
+      unsigned long long mk[kPullUnroll];
 #pragma unroll
-      for (int i = 0; i < kUnroll; i++) {
+      for (int i = 0; i < kPullUnroll; i++) {
         const int j = live ? __ffs(live) - 1 : 0;
         const bool ok = live != 0;
         live &= live - 1;
@@ -390,13 +392,13 @@ __device__ __forceinline__ void pull_min(const int32_t* __restrict__ t_col, cons
         if (!ok) mk[i] = 0ull;
       }
 #pragma unroll
-      for (int i = 0; i < kUnroll; i++) {
+      for (int i = 0; i < kPullUnroll; i++) {
         const int32_t* du = D + (size_t)(u[i] < 0 ? 0 : u[i]) * kBatch;
         dA[i] = (mk[i] >> lane) & 1ull ? __ldcg(du + lane) : 0x7fffffff;
         dB[i] = (mk[i] >> (lane + 32)) & 1ull ? __ldcg(du + lane + 32) : 0x7fffffff;
       }
 #pragma unroll
-      for (int i = 0; i < kUnroll; i++) {
+      for (int i = 0; i < kPullUnroll; i++) {
         if ((mk[i] >> lane) & 1ull) minA = min(minA, relax(dA[i], w[i], fl));
         if ((mk[i] >> (lane + 32)) & 1ull) minB = min(minB, relax(dB[i], w[i], fl));
       }
