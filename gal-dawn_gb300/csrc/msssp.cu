@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
 // Heavy rows are cut into pull_seg-entry segment tasks, each a warp, which
 // lower the row with return-free atomicMin where they improve on it and
 // OR their improved sources into the next mask (the first setter queues
-// the vertex).  Lane i owns sources i and i + 32, as in the push.  Tails
+// the vertex).  Lane i owns sources 2i and 2i + 1 (the push: i and i + 32).  Tails
 // are read 32 at a time (vertex, weight and mask coalesced or gathered once
 // per lane), then four distance rows are fetched before any is used.
 // Reading a row that another warp lowers in the same level is harmless:
@@ -367,10 +367,12 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
 // now is relaxed again at the next level through the mask it sets.
 constexpr int kPullUnroll = 4;  // distance rows of the pull fetched together
 
+// Lane i of the pull owns the adjacent sources 2i and 2i + 1, so a tail
+// row arrives as one 8-byte load per lane (one 256-byte request per warp).
 __device__ __forceinline__ void pull_min(const int32_t* __restrict__ t_col, const int32_t* __restrict__ t_w,
                                          const unsigned long long* __restrict__ m_in,
                                          const int32_t* __restrict__ D, bool fl, int k0, int k1,
-                                         int32_t& minA, int32_t& minB) {
+                                         int32_t& minE, int32_t& minO) {
   const int lane = lane_id();
   for (int kb = k0; kb < k1; kb += 32) {
     const int k = kb + lane;
@@ -379,8 +381,9 @@ __device__ __forceinline__ void pull_min(const int32_t* __restrict__ t_col, cons
     const unsigned long long cm = cu >= 0 ? __ldcg(m_in + cu) : 0ull;
     unsigned live = __ballot_sync(kFull, cm != 0ull);
     while (live) {
-      int32_t u[kPullUnroll], w[kPullUnroll], dA[kPullUnroll], dB[kPullUnroll];
-      unsigned long long mk[kPullUnroll];
+      int32_t u[kPullUnroll], w[kPullUnroll];
+      int2 d[kPullUnroll];
+      unsigned pair[kPullUnroll];
 #pragma unroll
       for (int i = 0; i < kPullUnroll; i++) {
         const int j = live ? __ffs(live) - 1 : 0;
@@ -388,22 +391,33 @@ __device__ __forceinline__ void pull_min(const int32_t* __restrict__ t_col, cons
         live &= live - 1;
         u[i] = __shfl_sync(kFull, cu, j);
         w[i] = __shfl_sync(kFull, cw, j);
-        mk[i] = __shfl_sync(kFull, cm, j);
-        if (!ok) mk[i] = 0ull;
+        const unsigned long long mk = __shfl_sync(kFull, cm, j);
+        pair[i] = ok ? (unsigned)(mk >> (2 * lane)) & 3u : 0u;
       }
 #pragma unroll
       for (int i = 0; i < kPullUnroll; i++) {
-        const int32_t* du = D + (size_t)(u[i] < 0 ? 0 : u[i]) * kBatch;
-        dA[i] = (mk[i] >> lane) & 1ull ? __ldcg(du + lane) : 0x7fffffff;
-        dB[i] = (mk[i] >> (lane + 32)) & 1ull ? __ldcg(du + lane + 32) : 0x7fffffff;
+        const int2* du = reinterpret_cast<const int2*>(D + (size_t)(u[i] < 0 ? 0 : u[i]) * kBatch) + lane;
+        d[i] = pair[i] ? __ldcg(du) : make_int2(0x7fffffff, 0x7fffffff);
       }
 #pragma unroll
       for (int i = 0; i < kPullUnroll; i++) {
-        if ((mk[i] >> lane) & 1ull) minA = min(minA, relax(dA[i], w[i], fl));
-        if ((mk[i] >> (lane + 32)) & 1ull) minB = min(minB, relax(dB[i], w[i], fl));
+        if (pair[i] & 1u) minE = min(minE, relax(d[i].x, w[i], fl));
+        if (pair[i] & 2u) minO = min(minO, relax(d[i].y, w[i], fl));
       }
     }
   }
+}
+
+// Bit i of x to bit 2i (the improved sources of the pull's even and odd
+// lanes back into source order).
+__device__ __forceinline__ unsigned long long spread_bits(unsigned v) {
+  unsigned long long x = v;
+  x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+  x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+  x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+  x = (x | (x << 2)) & 0x3333333333333333ull;
+  x = (x | (x << 1)) & 0x5555555555555555ull;
+  return x;
 }
 
 __global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__ row_ptr,
@@ -447,14 +461,15 @@ __global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__
     const int32_t v = __ldg(hv + lo);
     const int rbeg = t_row_ptr[v], rend = t_row_ptr[v + 1];
     const int ks = rbeg + (sidx - __ldg(hv_segoff + lo)) * pull_seg, ke = min(ks + pull_seg, rend);
-    int32_t minA = 0x7fffffff, minB = 0x7fffffff;
-    pull_min(t_col, t_w, m_in, D, fl, ks, ke, minA, minB);
-    int32_t* dv = D + (size_t)v * kBatch;
-    const bool impA = minA < __ldcg(dv + lane), impB = minB < __ldcg(dv + lane + 32);
-    if (impA) atomicMin(dv + lane, minA);
-    if (impB) atomicMin(dv + lane + 32, minB);
-    const unsigned long long bits = (unsigned long long)__ballot_sync(kFull, impA) |
-                                    ((unsigned long long)__ballot_sync(kFull, impB) << 32);
+    int32_t minE = 0x7fffffff, minO = 0x7fffffff;
+    pull_min(t_col, t_w, m_in, D, fl, ks, ke, minE, minO);
+    int32_t* dv = D + (size_t)v * kBatch + 2 * lane;
+    const int2 cur = __ldcg(reinterpret_cast<const int2*>(dv));
+    const bool impE = minE < cur.x, impO = minO < cur.y;
+    if (impE) atomicMin(dv, minE);
+    if (impO) atomicMin(dv + 1, minO);
+    const unsigned long long bits = spread_bits(__ballot_sync(kFull, impE)) |
+                                    (spread_bits(__ballot_sync(kFull, impO)) << 1);
     bool first = false;
     int deg = 0, rs = 0;
     if (bits && lane == 0) {
@@ -479,14 +494,14 @@ __global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__
     for (int j = 0; j < cnt; j++) {
       const int32_t v = __shfl_sync(kFull, mine, j);
       const int k0 = t_row_ptr[v], k1 = t_row_ptr[v + 1];
-      int32_t minA = 0x7fffffff, minB = 0x7fffffff;
-      pull_min(t_col, t_w, m_in, D, fl, k0, k1, minA, minB);
-      int32_t* dv = D + (size_t)v * kBatch;
-      const bool impA = minA < __ldcg(dv + lane), impB = minB < __ldcg(dv + lane + 32);
-      if (impA) dv[lane] = minA;
-      if (impB) dv[lane + 32] = minB;
-      const unsigned long long bits = (unsigned long long)__ballot_sync(kFull, impA) |
-                                      ((unsigned long long)__ballot_sync(kFull, impB) << 32);
+      int32_t minE = 0x7fffffff, minO = 0x7fffffff;
+      pull_min(t_col, t_w, m_in, D, fl, k0, k1, minE, minO);
+      int2* dv = reinterpret_cast<int2*>(D + (size_t)v * kBatch) + lane;
+      const int2 cur = __ldcg(dv);
+      const bool impE = minE < cur.x, impO = minO < cur.y;
+      if (impE || impO) *dv = make_int2(impE ? minE : cur.x, impO ? minO : cur.y);
+      const unsigned long long bits = spread_bits(__ballot_sync(kFull, impE)) |
+                                      (spread_bits(__ballot_sync(kFull, impO)) << 1);
       int deg = 0, rs = 0;
       if (bits) {
         if (lane == 0) m_out[v] = bits;
