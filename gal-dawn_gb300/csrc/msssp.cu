@@ -359,7 +359,9 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
 // Heavy rows are cut into pull_seg-entry segment tasks, each a warp, which
 // lower the row with return-free atomicMin where they improve on it and
 // OR their improved sources into the next mask (the first setter queues
-// the vertex).  Lane i owns sources 2i and 2i + 1 (the push: i and i + 32).  Tails
+// the vertex).  Lane i owns sources 2i and 2i + 1, so a distance row is one
+// 8-byte load per lane.  (The push keeps i and i + 32: its per-source
+// atomicMin instructions would otherwise span two 128-byte lines each.)  Tails
 // are read 32 at a time (vertex, weight and mask coalesced or gathered once
 // per lane), then four distance rows are fetched before any is used.
 // Reading a row that another warp lowers in the same level is harmless:
