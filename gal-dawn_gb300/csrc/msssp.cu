@@ -359,67 +359,129 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
 // Heavy rows are cut into pull_seg-entry segment tasks, each a warp, which
 // lower the row with return-free atomicMin where they improve on it and
 // OR their improved sources into the next mask (the first setter queues
-// the vertex).  Lane i owns sources 2i and 2i + 1, so a distance row is one
-// 8-byte load per lane.  (The push keeps i and i + 32: its per-source
-// atomicMin instructions would otherwise span two 128-byte lines each.)  Tails
-// are read 32 at a time (vertex, weight and mask coalesced or gathered once
-// per lane), then four distance rows are fetched before any is used.
+// the vertex).  A tail row (256 bytes) is read by a group of kRowLanes
+// lanes, kPullSrc sources (16 or 32 bytes) per lane, so one warp-wide load
+// brings kRowGroups rows.  Tails are read 32 at a time (vertex coalesced,
+// mask gathered once per lane); the live ones (mask not empty) are packed
+// with their weights into a per-warp shared-memory stage, and the groups
+// walk the stage kPullUnroll rows each, fetching those rows before any is
+// used.  Per-source minima stay in registers; the groups' minima are folded
+// at the end of the vertex and group 0 holds the result.
 // Reading a row that another warp lowers in the same level is harmless:
 // every value a row holds is the length of some path, and a value lowered
 // now is relaxed again at the next level through the mask it sets.
-constexpr int kPullUnroll = 4;  // distance rows of the pull fetched together
+// Eight sources per lane (four rows per warp-wide load) and three rows per
+// group in flight: 64 registers, four CTAs per SM.  RMAT scale 22 x 64
+// sources, int32: 29.3 ms with two sources per lane (one row per load,
+// tails passed by shuffles), 29.7 ms with four (two rows per load), 22.6
+// with eight and two rows per group, 22.3 with three; four rows per group
+// at three CTAs per SM 24.4 ms.
+constexpr int kPullSrc = 8;                 // sources per lane (4 or 8)
+constexpr int kPullUnroll = 3;              // rows per lane group fetched together
+constexpr int kRowLanes = kBatch / kPullSrc;  // lanes reading one tail row
+constexpr int kRowGroups = 32 / kRowLanes;    // tail rows per warp-wide load
+constexpr int kQuads = kPullSrc / 4;          // 16-byte pieces per lane and row
+static_assert(kPullSrc == 4 || kPullSrc == 8, "a lane reads whole 16-byte pieces of a row");
 
-// Lane i of the pull owns the adjacent sources 2i and 2i + 1, so a tail
-// row arrives as one 8-byte load per lane (one 256-byte request per warp).
+// Quad q of lane `sub` of a group: sources quad_base(sub, q) .. + 3 (with
+// eight sources per lane the second quad sits in the row's upper half, so
+// each load instruction of a group covers 128 contiguous bytes).
+__device__ __forceinline__ int quad_base(int sub, int q) { return 4 * sub + q * (kBatch / kQuads); }
+
 __device__ __forceinline__ void pull_min(const int32_t* __restrict__ t_col, const int32_t* __restrict__ t_w,
                                          const unsigned long long* __restrict__ m_in,
                                          const int32_t* __restrict__ D, bool fl, int k0, int k1,
-                                         int32_t& minE, int32_t& minO) {
-  const int lane = lane_id();
+                                         int4* __restrict__ stage, int32_t (&mn)[kPullSrc]) {
+  const int lane = lane_id(), grp = lane / kRowLanes, sub = lane % kRowLanes;
   for (int kb = k0; kb < k1; kb += 32) {
     const int k = kb + lane;
     const int32_t cu = k < k1 ? __ldg(t_col + k) : -1;
-    const int32_t cw = k < k1 ? __ldg(t_w + k) : 0;
     const unsigned long long cm = cu >= 0 ? __ldcg(m_in + cu) : 0ull;
-    unsigned live = __ballot_sync(kFull, cm != 0ull);
-    while (live) {
-      int32_t u[kPullUnroll], w[kPullUnroll];
-      int2 d[kPullUnroll];
-      unsigned pair[kPullUnroll];
+    const unsigned live = __ballot_sync(kFull, cm != 0ull);
+    if (cm)
+      stage[__popc(live & lanemask_lt())] =
+          make_int4(cu, __ldg(t_w + k), (int)(unsigned)cm, (int)(unsigned)(cm >> 32));
+    __syncwarp();
+    const int cnt = __popc(live);
+    for (int r0 = 0; r0 < cnt; r0 += kRowGroups * kPullUnroll) {
+      int4 e[kPullUnroll];
+      unsigned bits[kPullUnroll];
+      int4 d[kPullUnroll][kQuads];
 #pragma unroll
       for (int i = 0; i < kPullUnroll; i++) {
-        const int j = live ? __ffs(live) - 1 : 0;
-        const bool ok = live != 0;
-        live &= live - 1;
-        u[i] = __shfl_sync(kFull, cu, j);
-        w[i] = __shfl_sync(kFull, cw, j);
-        const unsigned long long mk = __shfl_sync(kFull, cm, j);
-        pair[i] = ok ? (unsigned)(mk >> (2 * lane)) & 3u : 0u;
+        const int r = r0 + i * kRowGroups + grp;
+        e[i] = r < cnt ? stage[r] : make_int4(0, 0, 0, 0);
+        bits[i] = 0u;
+#pragma unroll
+        for (int q = 0; q < kQuads; q++) {
+          const int base = quad_base(sub, q);
+          const unsigned word = base >= 32 ? (unsigned)e[i].w : (unsigned)e[i].z;
+          bits[i] |= ((word >> (base & 31)) & 15u) << (4 * q);
+        }
       }
 #pragma unroll
       for (int i = 0; i < kPullUnroll; i++) {
-        const int2* du = reinterpret_cast<const int2*>(D + (size_t)(u[i] < 0 ? 0 : u[i]) * kBatch) + lane;
-        d[i] = pair[i] ? __ldcg(du) : make_int2(0x7fffffff, 0x7fffffff);
+        const int4* du = reinterpret_cast<const int4*>(D + (size_t)e[i].x * kBatch);
+#pragma unroll
+        for (int q = 0; q < kQuads; q++)
+          d[i][q] = ((bits[i] >> (4 * q)) & 15u) ? __ldcg(du + quad_base(sub, q) / 4) : make_int4(0, 0, 0, 0);
       }
 #pragma unroll
       for (int i = 0; i < kPullUnroll; i++) {
-        if (pair[i] & 1u) minE = min(minE, relax(d[i].x, w[i], fl));
-        if (pair[i] & 2u) minO = min(minO, relax(d[i].y, w[i], fl));
+#pragma unroll
+        for (int q = 0; q < kQuads; q++) {
+          const unsigned b = bits[i] >> (4 * q);
+          if (b & 1u) mn[4 * q + 0] = min(mn[4 * q + 0], relax(d[i][q].x, e[i].y, fl));
+          if (b & 2u) mn[4 * q + 1] = min(mn[4 * q + 1], relax(d[i][q].y, e[i].y, fl));
+          if (b & 4u) mn[4 * q + 2] = min(mn[4 * q + 2], relax(d[i][q].z, e[i].y, fl));
+          if (b & 8u) mn[4 * q + 3] = min(mn[4 * q + 3], relax(d[i][q].w, e[i].y, fl));
+        }
       }
     }
+    __syncwarp();
   }
+#pragma unroll
+  for (int off = kRowLanes; off < 32; off <<= 1)
+#pragma unroll
+    for (int t = 0; t < kPullSrc; t++) mn[t] = min(mn[t], __shfl_xor_sync(kFull, mn[t], off));
 }
 
-// Bit i of x to bit 2i (the improved sources of the pull's even and odd
-// lanes back into source order).
-__device__ __forceinline__ unsigned long long spread_bits(unsigned v) {
-  unsigned long long x = v;
-  x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
-  x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
-  x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
-  x = (x | (x << 2)) & 0x3333333333333333ull;
-  x = (x | (x << 1)) & 0x5555555555555555ull;
-  return x;
+// The pulled minima of vertex v against its row: group 0 lowers the row
+// (plain stores where the warp owns the row, atomicMin on heavy-row
+// segments) and the warp returns the 64-bit mask of improved sources.
+template <bool kAtomic>
+__device__ __forceinline__ unsigned long long pull_store(int32_t* __restrict__ D, int32_t v,
+                                                         const int32_t (&mn)[kPullSrc]) {
+  const int lane = lane_id(), sub = lane % kRowLanes;
+  unsigned lo = 0u, hi = 0u;
+  if (lane < kRowLanes) {
+    int4* dv = reinterpret_cast<int4*>(D + (size_t)v * kBatch);
+#pragma unroll
+    for (int q = 0; q < kQuads; q++) {
+      const int base = quad_base(sub, q);
+      const int4 cur = __ldcg(dv + base / 4);
+      const int32_t* m = mn + 4 * q;
+      const unsigned imp = (unsigned)(m[0] < cur.x) | (unsigned)(m[1] < cur.y) << 1 |
+                           (unsigned)(m[2] < cur.z) << 2 | (unsigned)(m[3] < cur.w) << 3;
+      if (imp) {
+        if (kAtomic) {
+          int32_t* p = D + (size_t)v * kBatch + base;
+          if (imp & 1u) atomicMin(p + 0, m[0]);
+          if (imp & 2u) atomicMin(p + 1, m[1]);
+          if (imp & 4u) atomicMin(p + 2, m[2]);
+          if (imp & 8u) atomicMin(p + 3, m[3]);
+        } else {
+          dv[base / 4] = make_int4(imp & 1u ? m[0] : cur.x, imp & 2u ? m[1] : cur.y, imp & 4u ? m[2] : cur.z,
+                                   imp & 8u ? m[3] : cur.w);
+        }
+      }
+      if (base >= 32) hi |= imp << (base & 31);
+      else lo |= imp << base;
+    }
+  }
+  lo = __reduce_or_sync(kFull, lo);
+  hi = __reduce_or_sync(kFull, hi);
+  return (unsigned long long)hi << 32 | lo;
 }
 
 __global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__ row_ptr,
@@ -432,6 +494,7 @@ __global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__
                                                   const int32_t* __restrict__ hv, const int32_t* __restrict__ hv_segoff,
                                                   int32_t hv_count, int32_t hv_segs, int32_t pull_seg, int32_t n) {
   __shared__ int32_t s_q[kBlock / 32][kWarpQueue];
+  __shared__ int4 s_stage[kBlock / 32][32];
   if (ctl->done || ctl->mode != kModePull) return;
   const int L = ctl->level;
   const int pout = L & 1;
@@ -444,6 +507,7 @@ __global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__
   }
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   const bool fl = is_float != 0;
+  int4* stage = s_stage[wib];
   WarpQueue wq(s_q[wib], q + (size_t)pout * n, &ctl->qsize[pout]);
   Seg* sout = segs + (size_t)pout * segcap;
   unsigned long long* lpack = &ctl->lpack[pout];
@@ -463,15 +527,11 @@ __global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__
     const int32_t v = __ldg(hv + lo);
     const int rbeg = t_row_ptr[v], rend = t_row_ptr[v + 1];
     const int ks = rbeg + (sidx - __ldg(hv_segoff + lo)) * pull_seg, ke = min(ks + pull_seg, rend);
-    int32_t minE = 0x7fffffff, minO = 0x7fffffff;
-    pull_min(t_col, t_w, m_in, D, fl, ks, ke, minE, minO);
-    int32_t* dv = D + (size_t)v * kBatch + 2 * lane;
-    const int2 cur = __ldcg(reinterpret_cast<const int2*>(dv));
-    const bool impE = minE < cur.x, impO = minO < cur.y;
-    if (impE) atomicMin(dv, minE);
-    if (impO) atomicMin(dv + 1, minO);
-    const unsigned long long bits = spread_bits(__ballot_sync(kFull, impE)) |
-                                    (spread_bits(__ballot_sync(kFull, impO)) << 1);
+    int32_t mn[kPullSrc];
+#pragma unroll
+    for (int t = 0; t < kPullSrc; t++) mn[t] = 0x7fffffff;
+    pull_min(t_col, t_w, m_in, D, fl, ks, ke, stage, mn);
+    const unsigned long long bits = pull_store<true>(D, v, mn);
     bool first = false;
     int deg = 0, rs = 0;
     if (bits && lane == 0) {
@@ -496,14 +556,11 @@ __global__ void __launch_bounds__(kBlock, 4) mw_pull(const int32_t* __restrict__
     for (int j = 0; j < cnt; j++) {
       const int32_t v = __shfl_sync(kFull, mine, j);
       const int k0 = t_row_ptr[v], k1 = t_row_ptr[v + 1];
-      int32_t minE = 0x7fffffff, minO = 0x7fffffff;
-      pull_min(t_col, t_w, m_in, D, fl, k0, k1, minE, minO);
-      int2* dv = reinterpret_cast<int2*>(D + (size_t)v * kBatch) + lane;
-      const int2 cur = __ldcg(dv);
-      const bool impE = minE < cur.x, impO = minO < cur.y;
-      if (impE || impO) *dv = make_int2(impE ? minE : cur.x, impO ? minO : cur.y);
-      const unsigned long long bits = spread_bits(__ballot_sync(kFull, impE)) |
-                                      (spread_bits(__ballot_sync(kFull, impO)) << 1);
+      int32_t mn[kPullSrc];
+#pragma unroll
+      for (int t = 0; t < kPullSrc; t++) mn[t] = 0x7fffffff;
+      pull_min(t_col, t_w, m_in, D, fl, k0, k1, stage, mn);
+      const unsigned long long bits = pull_store<false>(D, v, mn);
       int deg = 0, rs = 0;
       if (bits) {
         if (lane == 0) m_out[v] = bits;
