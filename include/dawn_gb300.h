@@ -131,9 +131,8 @@ dawn_status dawn_bfs_device(dawn_graph* g, const int32_t* sources,
  * kernels are loaded there, until the process exits), so a graph is limited to
  * DAWN_STATIC_MAX_VERTICES vertices and DAWN_STATIC_MAX_EDGES edges; larger
  * ones are rejected with DAWN_ERR_INVALID_ARG.  The first call on a device
- * looks up that device's block; make it before any stream capture.  Calls
- * that overlap on one device (two host threads, or two streams) share the
- * block and race: serialise them. */
+ * looks up that device's block.  Calls that overlap on one device (two host
+ * threads, or two streams) share the block and race: serialise them. */
 #define DAWN_STATIC_MAX_VERTICES (1 << 20)
 #define DAWN_STATIC_MAX_EDGES (1LL << 24)
 dawn_status dawn_bfs_static(const int32_t* row_ptr, const int32_t* col,
