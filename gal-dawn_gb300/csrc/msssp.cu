@@ -46,6 +46,7 @@ struct MwCtl {
   unsigned long long mf[2];
   int32_t level, done, batch, nsrc;
   int32_t mode;                 // kModePush or kModePull for the next level
+  int32_t force;                // 0 = decide per level; 2 = every level a pull, other values a push
   int32_t work, hwork;          // pull: dynamic work counters (light rows, heavy-row segments)
   int32_t n_pull;
   int32_t n_push, inits;       // inits: mw_init CTAs finished
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(kBlock) mw_clear(MwCtl* __restrict__ ctl, int3
     ctl->n_push = 0;
     ctl->n_pull = 0;
     ctl->inits = 0;
-    ctl->mode = kModePush;
+    ctl->mode = ctl->force == 2 ? kModePull : kModePush;
     ctl->work = 0;
     ctl->hwork = 0;
   }
@@ -591,7 +592,8 @@ __global__ void mw_decide(MwCtl* __restrict__ ctl, int32_t n, long long m, int c
     return;
   }
   // a frontier whose out-edges reach half the graph is relaxed by a pull
-  ctl->mode = can_pull && 2 * (long long)ctl->mf[pout] >= m ? kModePull : kModePush;
+  if (ctl->force) ctl->mode = ctl->force == 2 ? kModePull : kModePush;
+  else ctl->mode = can_pull && 2 * (long long)ctl->mf[pout] >= m ? kModePull : kModePush;
   ctl->work = 0;
   ctl->hwork = 0;
   ctl->qsize[pout ^ 1] = 0;
@@ -694,6 +696,7 @@ dawn_status sssp_batched(dawn_graph* g, const int32_t* sources, int32_t nsrc, vo
   DAWN_CUDA(cudaMemcpyAsync(g->mw_sources.p, sources, sizeof(int32_t) * nsrc, cudaMemcpyHostToDevice,
                             g->stream));
   MwCtl c = {};
+  c.force = g->force_variant;
   c.nsrc = nsrc;
   c.dist_base = static_cast<int32_t*>(d_dist);
   c.sources = g->mw_sources.as<int32_t>();

@@ -230,12 +230,14 @@ dawn_status dawn_closeness(dawn_graph* g, const int32_t* sources,
  *                          edges of unfinished vertices (default 4) */
 #define DAWN_OPT_BITSET_WIDTH 1
 #define DAWN_OPT_PUSH_RATIO 2
-/*   DAWN_OPT_FORCE_VARIANT every level of BFS traversals runs one variant:
- *                          0 = decide per level (default), 1 = sparse push,
- *                          2 = bitmap pull, 3 = dense push (batched bitset
- *                          only; single-source runs it as sparse push).
- *                          For recording the per-variant level timings the
- *                          selector is trained on; distances are unchanged. */
+/*   DAWN_OPT_FORCE_VARIANT every level of BFS and SSSP traversals runs one
+ *                          variant: 0 = decide per level (default), 1 =
+ *                          sparse push, 2 = bitmap pull, 3 = dense push
+ *                          (batched bitset only; the other traversals run
+ *                          it as sparse push).  For recording the
+ *                          per-variant level timings the selector is
+ *                          trained on, and for tests; distances are
+ *                          unchanged. */
 #define DAWN_OPT_FORCE_VARIANT 3
 /*   DAWN_OPT_SELECTOR_MARGIN the learned selector overrides the direction
  *                          heuristic only when it predicts the other variant

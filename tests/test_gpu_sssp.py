@@ -131,6 +131,37 @@ def test_forced_push_and_pull(force):
                     assert st.pull_levels == 0
 
 
+@pytest.mark.parametrize("force,seg", [(1, 0), (2, 0), (2, 128), (0, 128)])
+def test_batched_forced_push_and_pull(force, seg):
+    # the batched traversal (AUTO, 70 sources: a full and a ragged batch) with
+    # every level a push (1) or a pull (2), or chosen per level (0); a pull
+    # segment of 128 in-edges makes every in-row of 256 or more a heavy row
+    # cut into segment tasks, so the light and the heavy pull run side by
+    # side.  In-degrees from 0 to over a thousand leave every count of live
+    # tails per 32-entry batch and per lane group.
+    graphs = [
+        asym_weights(gen.rmat(14, 16, seed=61), 62),
+        gen.erdos_renyi(20000, 200000, seed=63, weights=True),
+        gen.rmat(16, 32, a=0.62, b=0.17, c=0.17, seed=64, weights=True),
+    ]
+    for g in graphs:
+        srcs = gen.sources(g, 70, seed=85, from_lcc=g.symmetric)
+        want = O.msssp(g, srcs)
+        for w in ("i32", "f32"):
+            with abi.Graph(g, weights=w) as dg:
+                dg.set_option(abi.OPT_FORCE_VARIANT, force)
+                if seg:
+                    dg.set_option(abi.OPT_PULL_SEGMENT, seg)
+                d, st = dg.sssp(srcs, variant=abi.VARIANT_AUTO)
+                bad = np.argwhere(to_ref(d) != want)
+                assert bad.size == 0, (force, seg, w, g.n, bad[:5])
+                assert st.batches == 2
+                if force == 2:
+                    assert st.pull_levels > 0 and st.push_levels == 0
+                if force == 1:
+                    assert st.pull_levels == 0 and st.push_levels > 0
+
+
 def test_pull_segment_sizes():
     g = gen.rmat(16, 32, a=0.62, b=0.17, c=0.17, seed=66, weights=True)
     srcs = gen.sources(g, 3, seed=67)
