@@ -64,15 +64,17 @@ L2_BYTES = 129 * 2 ** 20
 _CAPTURE = ("ncu launch list of one RMAT-22 x 64 step, bitset variant, traced form: "
             "dram__bytes_read.sum + dram__bytes_write.sum per launch")
 NCU_TRAFFIC = {
-    "bs_pull": {"bytes": 333.8e6, "launches": 5, "file": "gal-dawn_gb300/csrc/msbfs.cu", "sha": "46d6bbfdfa9da210",
+    "bs_pull": {"bytes": 337.6e6, "launches": 5, "file": "gal-dawn_gb300/csrc/msbfs.cu", "sha": "b34bab346d11c22d",
                 "source": _CAPTURE},
-    "bs_emit_dist": {"bytes": 1177.8e6, "launches": 1, "file": "gal-dawn_gb300/csrc/msbfs.cu",
-                     "sha": "46d6bbfdfa9da210", "source": _CAPTURE},
+    "bs_emit_dist": {"bytes": 1177.9e6, "launches": 1, "file": "gal-dawn_gb300/csrc/msbfs.cu",
+                     "sha": "b34bab346d11c22d", "source": _CAPTURE},
 }
 # L1/TEX global-load sectors of the level-3 pull (every in-edge unfinished)
-# from `ncu --set full` of the same build (143,753,817 sectors, 128,306,834
-# in-edges): the unit the pull is bound by moves about one sector per SM
-# clock, so sectors per in-edge x in-edges / (SMs x clock) bounds a level.
+# from `ncu --set full` of the 64-source pull (143,753,817 sectors,
+# 128,306,834 in-edges; build 46d6bbfdfa9da210, whose 64-source kernels are
+# the current ones): the unit the pull is bound by moves about one sector
+# per SM clock, so sectors per in-edge x in-edges / (SMs x clock) bounds a
+# level.
 PULL_SECTORS_PER_EDGE = 143753817 / 128306834
 
 

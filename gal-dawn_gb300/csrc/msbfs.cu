@@ -137,10 +137,16 @@ struct Bits {
     for (int i = 0; i < W; i++) b.w[i] = ctl->full[i];
     return b;
   }
-  // Vectorised loads: W = 2 is one 16-byte load, W = 4 two of them.
+  // Vectorised loads: W = 2 is one 16-byte load, W = 4 one 32-byte load
+  // (a gather then asks L1/TEX for its sector once, not twice).  The
+  // vertex's words start on a 32-byte boundary: slots are n x 32 bytes
+  // apart from an aligned base.
   __device__ __forceinline__ static Bits ldg(const u64* p) {
     Bits b;
-    if (W == 1) {
+    if constexpr (W == 4) {
+      asm("ld.global.nc.v4.u64 {%0,%1,%2,%3}, [%4];" : "=l"(b.w[0]), "=l"(b.w[1]), "=l"(b.w[2]), "=l"(b.w[3])
+          : "l"(p));
+    } else if (W == 1) {
       b.w[0] = __ldg(p);
     } else {
 #pragma unroll
