@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
 // from tails whose source s improved at the last level, and keeps it where
 // it beats D[v][s].  A warp owns a light row (in-degree below 2 x pull_seg)
 // and writes its row of D and its next mask with plain stores: no atomics
-// per edge, and one improvement ballot per vertex instead of per edge.
+// per edge, and one improved-source mask per vertex instead of per edge.
 // Heavy rows are cut into pull_seg-entry segment tasks, each a warp, which
 // lower the row with return-free atomicMin where they improve on it and
 // OR their improved sources into the next mask (the first setter queues
