@@ -223,12 +223,63 @@ __device__ __forceinline__ void relax_row(const int32_t* __restrict__ row_ptr, c
   }
 }
 
+// A long-row segment (at most kSeg entries) of a vertex active for few
+// sources: the lanes take 32 consecutive edges at a time and relax each of
+// the vertex's active sources along them, so a segment costs
+// ceil(len / 32) rounds per source instead of the len / kUnroll rounds of
+// the warp-per-edge form, whose lanes mostly idle on such a mask (the hubs
+// next to the sources at the first levels).  All 32 lanes call it with the
+// same arguments.
+__device__ __forceinline__ void relax_seg_sparse(const int32_t* __restrict__ row_ptr,
+                                                 const int32_t* __restrict__ col, const int32_t* __restrict__ w,
+                                                 bool fl, int32_t* __restrict__ D,
+                                                 unsigned long long* __restrict__ m_out, int32_t u, int k0, int k1,
+                                                 unsigned long long mask, WarpQueue& wq, Seg* __restrict__ sout,
+                                                 unsigned long long* lpack, unsigned long long& my_mf) {
+  const int lane = lane_id();
+  const int32_t* du = D + (size_t)u * kBatch;
+  for (int kb = k0; kb < k1; kb += 32) {
+    const int k = kb + lane;
+    const int32_t v = k < k1 ? __ldg(col + k) : -1;
+    const int32_t wv = k < k1 ? __ldg(w + k) : 0;
+    const int32_t* dv = D + (size_t)(v < 0 ? 0 : v) * kBatch;
+    unsigned long long mine = 0ull;
+    for (unsigned long long m = mask; m; m &= m - 1) {
+      const int src = __ffsll((long long)m) - 1;
+      const int32_t dsu = __ldcg(du + src);
+      if (v >= 0) {
+        const int32_t c = relax(dsu, wv, fl);
+        if (c < __ldcg(dv + src)) {
+          atomicMin(D + (size_t)v * kBatch + src, c);
+          mine |= 1ull << src;
+        }
+      }
+    }
+    bool first = false;
+    int deg = 0, rs = 0;
+    if (mine) {
+      first = atomicOr(m_out + v, mine) == 0ull;
+      if (first) {
+        rs = row_ptr[v];
+        deg = row_ptr[v + 1] - rs;
+        my_mf += (unsigned long long)deg;
+      }
+    }
+    emit_routed(first, v, deg, rs, wq, sout, lpack);
+  }
+}
+
 // Frontier vertices whose mask holds at most kSparse sources (the waves of
 // different sources crossing a high-diameter graph: most vertices are
 // active for one or two of the 64 at a time) go through pairs instead of a
 // warp per vertex: one lane per (vertex, improved source), relaxing that
 // source along the vertex's row with kUnroll targets in flight.
 constexpr int kSparse = 16;
+// Long-row segments go edge-parallel up to this many active sources.
+// RMAT scale 22 x 64, int32, same host: 22.4 -> 21.2 ms (level 1, the
+// sources' hub neighbours, 1.86 -> 0.87 ms); thresholds 2, 8 and 16 within
+// 0.1%.
+constexpr int kSparseSeg = 8;
 
 // One level.  Warp tasks: the long-row segments (a warp each), then the
 // input queue 32 vertices at a time: the vertices with dense masks get the
@@ -266,7 +317,11 @@ __global__ void __launch_bounds__(kBlock, 4) mw_push(const int32_t* __restrict__
     if (t < ln) {
       const Seg sg = sin[t];
       const int k1 = min(sg.k0 + kSeg, row_ptr[sg.v + 1]);
-      relax_row(row_ptr, col, w, fl, D, m_out, sg.v, sg.k0, k1, __ldcg(m_in + sg.v), wq, sout, lpack, my_mf);
+      const unsigned long long sm = __ldcg(m_in + sg.v);
+      if (__popcll(sm) <= kSparseSeg)
+        relax_seg_sparse(row_ptr, col, w, fl, D, m_out, sg.v, sg.k0, k1, sm, wq, sout, lpack, my_mf);
+      else
+        relax_row(row_ptr, col, w, fl, D, m_out, sg.v, sg.k0, k1, sm, wq, sout, lpack, my_mf);
       continue;
     }
     const int i = (t - ln) * 32 + lane;
