@@ -64,10 +64,10 @@ L2_BYTES = 129 * 2 ** 20
 _CAPTURE = ("ncu launch list of one RMAT-22 x 64 step, bitset variant, traced form: "
             "dram__bytes_read.sum + dram__bytes_write.sum per launch")
 NCU_TRAFFIC = {
-    "bs_pull": {"bytes": 337.6e6, "launches": 5, "file": "gal-dawn_gb300/csrc/msbfs.cu", "sha": "b34bab346d11c22d",
+    "bs_pull": {"bytes": 337.8e6, "launches": 5, "file": "gal-dawn_gb300/csrc/msbfs.cu", "sha": "8765e77b47788482",
                 "source": _CAPTURE},
-    "bs_emit_dist": {"bytes": 1177.9e6, "launches": 1, "file": "gal-dawn_gb300/csrc/msbfs.cu",
-                     "sha": "b34bab346d11c22d", "source": _CAPTURE},
+    "bs_emit_dist": {"bytes": 1178.3e6, "launches": 1, "file": "gal-dawn_gb300/csrc/msbfs.cu",
+                     "sha": "8765e77b47788482", "source": _CAPTURE},
 }
 # L1/TEX global-load sectors of the level-3 pull (every in-edge unfinished)
 # from `ncu --set full` of the 64-source pull (143,753,817 sectors,

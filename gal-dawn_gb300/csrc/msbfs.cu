@@ -61,7 +61,7 @@ struct BsCtl {
   long long mu;                 // in-degree sum of vertices not yet finished
   long long mu_dec;             // in-degree of vertices finished this level
   unsigned long long reached;   // TEPS numerator of the batch
-  unsigned long long full[kMaxW];  // this batch's source bits
+  unsigned long long full[kMaxW];  // this batch's source bits, less those of sources without out-edges
   int32_t* dist_base;
   const int32_t* sources;
   int32_t* lv_block;            // level mode: n x 64 levels, vertex-major (else NULL)
@@ -402,7 +402,13 @@ __global__ void bs_init(BsCtl* __restrict__ ctl, const int32_t* __restrict__ row
     const u64 bit = 1ull << (b & 63);
     atomicOr(visit + (size_t)s * W + (b >> 6), bit);
     atomicOr(fr0 + (size_t)s * W + (b >> 6), bit);
-    atomicAdd(&s_reached, (u64)(row_ptr[s + 1] - row_ptr[s]));
+    const int deg = row_ptr[s + 1] - row_ptr[s];
+    atomicAdd(&s_reached, (u64)deg);
+    // A source without out-edges reaches no vertex but itself.  Its bit is
+    // left out of `full`, so the other vertices still finish (and leave
+    // the pull lists) once every other source has reached them; a batch
+    // of all vertices as sources holds many such sources.
+    if (deg == 0) atomicAnd(&ctl->full[b >> 6], ~bit);
   }
   __syncthreads();
   // A vertex that is the source of several bits is queued once, by the
