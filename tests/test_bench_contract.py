@@ -56,6 +56,13 @@ def test_traffic_only_for_the_captured_build(monkeypatch):
     assert bench.ncu_traffic("bs_push_update") is None
 
 
+def test_committed_traffic_matches_the_committed_kernels():
+    # a kernel file changed without a new ncu capture would report traffic
+    # null in the bench line: the capture and its constants go with the change
+    for kernel, t in bench.NCU_TRAFFIC.items():
+        assert bench.ncu_traffic(kernel) is not None, (kernel, t["file"], bench._source_hash(t["file"]), t["sha"])
+
+
 def test_reached_edges():
     import numpy as np
     deg = np.array([3, 1, 0, 2], np.int64)
