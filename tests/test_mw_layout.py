@@ -71,3 +71,30 @@ def test_init_marker_last_entry_wins(seed):
         if d[cols[k]] == -(k + 1):
             d[cols[k]] = weights[k]
     assert np.array_equal(d, got)
+
+
+def test_sparse_segment_relaxes_every_edge_source_pair_once():
+    # relax_seg_sparse (mw_push): the lanes take 32 consecutive edges of the
+    # segment at a time and walk the vertex's active sources in bit order;
+    # every (edge, active source) pair is relaxed once, and each lane's
+    # improved sources reach the target's mask in one OR
+    rng = np.random.default_rng(9)
+    for _ in range(50):
+        k0 = int(rng.integers(0, 1000))
+        k1 = k0 + int(rng.integers(1, 129))  # a segment holds at most 128 entries
+        mask = 0
+        for s in rng.choice(64, int(rng.integers(1, 9)), replace=False):
+            mask |= 1 << int(s)
+        seen = {}
+        for kb in range(k0, k1, 32):
+            for lane in range(32):
+                k = kb + lane
+                if k >= k1:
+                    continue
+                m = mask
+                while m:
+                    src = (m & -m).bit_length() - 1
+                    m &= m - 1
+                    seen[(k, src)] = seen.get((k, src), 0) + 1
+        want = {(k, s) for k in range(k0, k1) for s in range(64) if (mask >> s) & 1}
+        assert set(seen) == want and set(seen.values()) == {1}
